@@ -1,0 +1,366 @@
+"""ctypes binding of the libepseon_cuda C ABI (``include/epscu.h``).
+
+This is the thin Python view of the same entry points a cgo/JNI/ctypes user
+would bind; the parity tests call the solver through it.  There is no CPU
+fallback: if the CUDA library is missing or no device is present, every call
+raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _build
+
+EPSCU_OK = 0
+ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_CANCELLED, ERR_CAPACITY, ERR_TIMEOUT = 1, 2, 3, 4, 5, 6
+LEVEL_OK, LEVEL_MAXITER, LEVEL_NONFINITE, LEVEL_UNDER_RESOLVED = 0, 1, 2, 4
+LEVEL_CANCELLED, LEVEL_NOT_FOUND, LEVEL_BAD_INPUT = 8, 16, 32
+METHOD_PLAIN_FP64, METHOD_FAST_FP32C = 0, 1
+KIND_MORSE, KIND_LJ, KIND_SPLINE = 0, 1, 2
+MEM_DEVICE, WANT_PSI, STAGE_TIMING = 1, 2, 4
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+_lp = C.POINTER(C.c_int64)
+
+
+class Batch(C.Structure):
+    _fields_ = [
+        ("n_potentials", C.c_int32),
+        ("V", _dp),
+        ("offsets", _lp),
+        ("N", _ip),
+        ("r_min", _dp),
+        ("r_max", _dp),
+        ("mu", _dp),
+        ("e_cap", _dp),
+        ("n_trial", C.c_int32),
+        ("min_level", C.c_int32),
+        ("max_level", C.c_int32),
+    ]
+
+
+class Opts(C.Structure):
+    _fields_ = [
+        ("method", C.c_int32),
+        ("flags", C.c_int32),
+        ("tol", C.c_double),
+        ("stream", C.c_void_p),
+        ("tune", C.c_int32),
+        ("reserved", C.c_int32),
+    ]
+
+
+class Result(C.Structure):
+    _fields_ = [
+        ("level_capacity", C.c_int32),
+        ("n_total", _ip),
+        ("n_out", _ip),
+        ("energy", _dp),
+        ("nodes", _ip),
+        ("status", _ip),
+        ("err_est", _dp),
+        ("psi", _dp),
+        ("psi_capacity", C.c_int64),
+        ("psi_offsets", _lp),
+        ("psi_required", C.c_int64),
+    ]
+
+
+class DeviceInfo(C.Structure):
+    _fields_ = [
+        ("name", C.c_char * 256),
+        ("ordinal", C.c_int32),
+        ("pci_device_id", C.c_int32),
+        ("pci_bus_id", C.c_int32),
+        ("cc_major", C.c_int32),
+        ("cc_minor", C.c_int32),
+        ("sm_count", C.c_int32),
+        ("total_global_mem", C.c_int64),
+        ("shared_mem_per_block_optin", C.c_int32),
+        ("max_threads_per_block", C.c_int32),
+        ("max_grid_dim", C.c_int32 * 3),
+        ("max_block_dim", C.c_int32 * 3),
+        ("l2_cache_size", C.c_int32),
+        ("driver_version", C.c_int32),
+        ("runtime_version", C.c_int32),
+        ("uuid", C.c_uint8 * 16),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("ms_prepare", C.c_float),
+        ("ms_scan", C.c_float),
+        ("ms_refine32", C.c_float),
+        ("ms_polish64", C.c_float),
+        ("ms_write", C.c_float),
+        ("ms_total", C.c_float),
+        ("scan_point_updates", C.c_int64),
+        ("refine_point_updates", C.c_int64),
+        ("fp64_point_updates", C.c_int64),
+        ("psi_bytes", C.c_int64),
+        ("n_levels", C.c_int64),
+        ("kernel_launches", C.c_int32),
+        ("fallbacks", C.c_int32),
+    ]
+
+
+# every symbol the header declares (checked by the CPU test suite)
+EXPORTED = [
+    "epscu_abi_version",
+    "epscu_device_count",
+    "epscu_get_device_info",
+    "epscu_last_error",
+    "epscu_create",
+    "epscu_destroy",
+    "epscu_set_arena_block",
+    "epscu_solve",
+    "epscu_adjoint",
+    "epscu_tabulate",
+    "epscu_cancel",
+    "epscu_last_stats",
+    "epscu_measure_fma_peaks",
+]
+
+_lib = None
+
+
+class EpscuError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"epscu error {code}: {msg}")
+        self.code = code
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load libepseon_cuda.so (building it in-tree first if it is absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_build.LIB):
+        if not build_if_missing:
+            raise OSError(f"{_build.LIB} is not built")
+        _build.build_cuda()
+    L = C.CDLL(_build.LIB)
+    L.epscu_abi_version.restype = C.c_int32
+    L.epscu_last_error.restype = C.c_char_p
+    L.epscu_device_count.argtypes = [_ip]
+    L.epscu_get_device_info.argtypes = [C.c_int32, C.POINTER(DeviceInfo)]
+    L.epscu_create.argtypes = [C.c_int32, C.POINTER(C.c_void_p)]
+    L.epscu_destroy.argtypes = [C.c_void_p]
+    L.epscu_set_arena_block.argtypes = [C.c_void_p, C.c_int64]
+    L.epscu_solve.argtypes = [C.c_void_p, C.POINTER(Batch), C.POINTER(Result), C.POINTER(Opts)]
+    L.epscu_adjoint.argtypes = [C.c_void_p, _dp, _dp, C.c_int32, C.POINTER(Opts)]
+    L.epscu_tabulate.argtypes = [C.c_void_p, C.c_int32, _ip, _dp, _lp, _ip, _dp, _dp, C.c_int32, _dp, C.POINTER(Opts)]
+    L.epscu_cancel.argtypes = [C.c_void_p]
+    L.epscu_last_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
+    L.epscu_measure_fma_peaks.argtypes = [C.c_void_p, _dp, _dp]
+    for name in EXPORTED:
+        if name not in ("epscu_abi_version", "epscu_last_error"):
+            getattr(L, name).restype = C.c_int32
+    _lib = L
+    return L
+
+
+def _check(code: int):
+    if code != EPSCU_OK:
+        raise EpscuError(code, load().epscu_last_error().decode(errors="replace"))
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
+
+
+def _l(a):
+    return a.ctypes.data_as(_lp)
+
+
+def device_count() -> int:
+    c = C.c_int32()
+    rc = load().epscu_device_count(C.byref(c))
+    return c.value if rc == EPSCU_OK else 0
+
+
+def device_info(ordinal: int) -> DeviceInfo:
+    info = DeviceInfo()
+    _check(load().epscu_get_device_info(ordinal, C.byref(info)))
+    return info
+
+
+@dataclass
+class Solution:
+    """Levels of a batch in [potential x capacity] layout (slot s = level min_level + s)."""
+
+    n_total: np.ndarray
+    n_out: np.ndarray
+    energy: np.ndarray
+    nodes: np.ndarray
+    status: np.ndarray
+    err_est: np.ndarray
+    psi: np.ndarray | None
+    psi_offsets: np.ndarray
+    N: np.ndarray
+
+    def levels(self, p: int) -> np.ndarray:
+        return self.energy[p, : self.n_out[p]]
+
+    def wavefunctions(self, p: int) -> np.ndarray:
+        o = int(self.psi_offsets[p])
+        n, N = int(self.n_out[p]), int(self.N[p])
+        return self.psi[o : o + n * N].reshape(n, N)
+
+
+def concat(Vs):
+    N = np.array([v.size for v in Vs], np.int32)
+    offsets = np.zeros(len(Vs), np.int64)
+    offsets[1:] = np.cumsum(N[:-1].astype(np.int64))
+    return np.ascontiguousarray(np.concatenate([np.asarray(v, np.float64) for v in Vs])), offsets, N
+
+
+class Context:
+    """One epscu context on one device."""
+
+    def __init__(self, device: int = 0):
+        self._lib = load()
+        self._h = C.c_void_p()
+        _check(self._lib.epscu_create(int(device), C.byref(self._h)))
+        self.device = device
+
+    def close(self):
+        if self._h:
+            self._lib.epscu_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_arena_block(self, nbytes: int):
+        _check(self._lib.epscu_set_arena_block(self._h, int(nbytes)))
+
+    def cancel(self):
+        _check(self._lib.epscu_cancel(self._h))
+
+    def stats(self) -> Stats:
+        s = Stats()
+        _check(self._lib.epscu_last_stats(self._h, C.byref(s)))
+        return s
+
+    def measure_fma_peaks(self):
+        a, b = C.c_double(), C.c_double()
+        _check(self._lib.epscu_measure_fma_peaks(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def solve(
+        self,
+        Vs,
+        r_min,
+        r_max,
+        mu,
+        e_cap,
+        n_trial: int,
+        method: int = METHOD_FAST_FP32C,
+        min_level: int = 0,
+        max_level: int = -1,
+        level_capacity: int | None = None,
+        want_psi: bool = False,
+        psi_capacity: int | None = None,
+        tol: float = 1e-12,
+        tune: bool = False,
+    ) -> Solution:
+        """Solve a batch of host potentials (host buffers through the C ABI)."""
+        V, offsets, N = concat(Vs)
+        n = len(Vs)
+
+        def arr(x):
+            a = np.asarray(x, np.float64)
+            return np.ascontiguousarray(np.broadcast_to(a, (n,)) if a.ndim == 0 else a)
+
+        r_min, r_max, mu, e_cap = arr(r_min), arr(r_max), arr(mu), arr(e_cap)
+        if level_capacity is None:
+            level_capacity = (max_level - min_level + 1) if max_level >= 0 else 512
+        cap = int(level_capacity)
+        n_total = np.zeros(n, np.int32)
+        n_out = np.zeros(n, np.int32)
+        energy = np.zeros((n, cap))
+        nodes = np.zeros((n, cap), np.int32)
+        status = np.zeros((n, cap), np.int32)
+        err = np.zeros((n, cap))
+        psi_off = np.zeros(n, np.int64)
+        psi = None
+        if want_psi:
+            if psi_capacity is None:
+                psi_capacity = int(N.astype(np.int64).sum()) * cap
+            psi = np.zeros(int(psi_capacity))
+        b = Batch(n, _d(V), _l(offsets), _i(N), _d(r_min), _d(r_max), _d(mu), _d(e_cap), int(n_trial), int(min_level), int(max_level))
+        r = Result(
+            cap,
+            _i(n_total),
+            _i(n_out),
+            _d(energy),
+            _i(nodes),
+            _i(status),
+            _d(err),
+            _d(psi) if psi is not None else None,
+            int(psi.size) if psi is not None else 0,
+            _l(psi_off),
+            0,
+        )
+        o = Opts(int(method), WANT_PSI if want_psi else 0, float(tol), None, 1 if tune else 0, 0)
+        _check(self._lib.epscu_solve(self._h, C.byref(b), C.byref(r), C.byref(o)))
+        return Solution(n_total, n_out, energy, nodes, status, err, psi, psi_off, N)
+
+    def adjoint(self, dL_dE: np.ndarray, total_points: int, recompute: bool = False) -> np.ndarray:
+        g = np.ascontiguousarray(dL_dE, np.float64)
+        out = np.zeros(int(total_points))
+        o = Opts(0, 0, 0.0, None, 0, 0)
+        _check(self._lib.epscu_adjoint(self._h, _d(g), _d(out), 1 if recompute else 0, C.byref(o)))
+        return out
+
+    def tabulate(self, kind, params, N, r_min, r_max, n_knots: int = 1024) -> list:
+        kind = np.ascontiguousarray(kind, np.int32)
+        params = np.ascontiguousarray(params, np.float64).reshape(-1, 12)
+        N = np.ascontiguousarray(N, np.int32)
+        offsets = np.zeros(N.size, np.int64)
+        offsets[1:] = np.cumsum(N[:-1].astype(np.int64))
+        r_min = np.ascontiguousarray(r_min, np.float64)
+        r_max = np.ascontiguousarray(r_max, np.float64)
+        V = np.zeros(int(N.astype(np.int64).sum()))
+        o = Opts(0, 0, 0.0, None, 0, 0)
+        _check(
+            self._lib.epscu_tabulate(
+                self._h, int(N.size), _i(kind), _d(params), _l(offsets), _i(N), _d(r_min), _d(r_max), int(n_knots), _d(V), C.byref(o)
+            )
+        )
+        return [V[offsets[i] : offsets[i] + N[i]] for i in range(N.size)]
+
+
+def batch_params(b) -> np.ndarray:
+    """[n, 12] parameter rows of a synth.PotentialBatch for epscu_tabulate."""
+    n = len(b)
+    P = np.zeros((n, 12))
+    for i in range(n):
+        if int(b.kind[i]) == KIND_LJ:
+            P[i, 0:2] = b.lj[i]
+        else:
+            P[i, 0:3] = b.morse[i]
+            P[i, 3:12] = b.bumps[i].reshape(-1)
+    return P

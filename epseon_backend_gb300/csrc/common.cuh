@@ -1,0 +1,170 @@
+// common.cuh -- device-side data layout and arithmetic shared by the solver
+// kernels of libepseon_cuda (sm_103a).
+//
+// The discrete problem is the one the FP64 oracle restates (Numerov on a
+// uniform grid with E-independent Dirichlet cut-offs, twisted Sturm counts):
+//   a = mu h^2 / 6,  T_i = aE - W_i with W_i = a V_i,  f_i = 1 + T_i,
+//   g_i = 2 - 10 T_i,  projective step (A, B) <- (g A - f B, f A).
+// Every FP64 expression on the count/bisection path is written with explicit
+// __dadd_rn/__dmul_rn/__fma_rn so that nvcc cannot contract it differently
+// from the oracle's explicit fma() calls.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "epscu.h"
+
+// status bits kept per potential / level (public values from epscu.h)
+#define EPSCU_STATUS_MAXITER EPSCU_LEVEL_MAXITER
+#define EPSCU_STATUS_NONFINITE EPSCU_LEVEL_NONFINITE
+#define EPSCU_STATUS_UNDER EPSCU_LEVEL_UNDER_RESOLVED
+#define EPSCU_STATUS_CANCELLED EPSCU_LEVEL_CANCELLED
+#define EPSCU_STATUS_NOTFOUND EPSCU_LEVEL_NOT_FOUND
+#define EPSCU_STATUS_BAD EPSCU_LEVEL_BAD_INPUT
+
+namespace epscu {
+
+constexpr int kRenorm = 32;  // renormalise the projective state every kRenorm steps
+
+// Per-potential constants, written by the prepare kernel.
+struct PotMeta {
+    double r_min, r_max, mu, e_cap;  // inputs
+    double h, a, e_lo, delta;        // derived (same formulas as the oracle)
+    int64_t off;                     // first element in V64 / W64 / Msuf
+    int64_t offf;                    // first element in Wf2 (tile aligned)
+    int64_t psi_off;                 // first element of this potential's psi rows
+    int32_t N, i0, i1, k_scan;
+    int32_t n_bisect, n_trial;
+    int32_t n_total, n_out;
+    int32_t level_base, status;
+    int32_t pad0, pad1;
+};
+
+// One level slot of the refinement stages.
+struct LevelWork {
+    double lo, hi;      // bracket (count(lo) <= v < count(hi))
+    double E;           // current energy
+    double dE;          // last correction (error estimate)
+    double norm_k_out;  // write-pass constants: psi scale on the outward side
+    double norm_k_in;   //   and on the inward side
+    double ck;          // psi at the match index
+    int32_t ex_out, ex_in;  // binary exponents of the two side constants
+    int32_t p, v;
+    int32_t nodes, status;
+    int32_t k;          // match index used by the write pass
+    int32_t iters;
+};
+
+// Global counters and flags of one solve (device memory).
+struct Header {
+    int32_t total_levels;
+    int32_t queue_scan;
+    int32_t queue_refine;
+    int32_t queue_polish;
+    int32_t error;          // first device-side error code (0 = none)
+    int32_t fallbacks;
+    int32_t pad[2];
+};
+
+// ---------------------------------------------------------------- FP64 helpers
+
+// One divide-free projective Numerov step (identical to the oracle's
+// numerov_step): state (A, B) ~ s (u_i, u_{i-1}) -> s f_i (u_{i+1}, u_i).
+__device__ __forceinline__ void step64(double aE, double w, double& A, double& B) {
+    const double T = __dsub_rn(aE, w);
+    const double f = __dadd_rn(1.0, T);
+    const double g = __fma_rn(-10.0, T, 2.0);
+    const double An = __fma_rn(g, A, -__dmul_rn(f, B));
+    B = __dmul_rn(f, A);
+    A = An;
+}
+
+// frexp-style exponent of |m| (m = f 2^e, f in [0.5, 1)) for finite normal m.
+__device__ __forceinline__ int exp_of(double m) {
+    const int hi = __double2hiint(m);
+    return ((hi >> 20) & 0x7ff) - 1022;
+}
+
+// Exact power of two 2^e for |e| < 1000.
+__device__ __forceinline__ double pow2(int e) { return __hiloint2double((1023 + e) << 20, 0); }
+
+// Rescale (x, y) by the power of two that brings max(|x|,|y|) into [0.5, 1);
+// returns the exponent removed (0 when the pair is zero or not finite).
+__device__ __forceinline__ int renorm_pair(double& x, double& y) {
+    const double m = fmax(fabs(x), fabs(y));
+    if (!(m > 0.0) || !isfinite(m)) return 0;
+    const int e = exp_of(m);
+    if (e > 1000 || e < -1000) return 0;
+    const double s = pow2(-e);
+    x *= s;
+    y *= s;
+    return e;
+}
+
+// E_j = E_lo + (j+1) delta (two roundings, as in the oracle).
+__device__ __forceinline__ double trial_energy(const PotMeta& m, int j) {
+    return __dadd_rn(m.e_lo, __dmul_rn((double)(j + 1), m.delta));
+}
+
+// Largest i in [i0, i1] with V_i <= E, by binary search on the suffix minima
+// Msuf_i = min(V_i .. V_{i1}); k_scan when there is none.  Equals the
+// oracle's linear search.
+__device__ __forceinline__ int match_index(const PotMeta& m, const double* __restrict__ Msuf, double E) {
+    const double* M = Msuf + m.off;
+    if (!(M[m.i0] <= E)) return m.k_scan;
+    int lo = m.i0, hi = m.i1;  // invariant: M[lo] <= E
+    while (lo < hi) {
+        const int mid = lo + (hi - lo + 1) / 2;
+        if (M[mid] <= E) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Twisted Sturm count at E with twist index k (identical arithmetic to the
+// oracle's eo_count).
+__device__ __forceinline__ int count64(const PotMeta& m, const double* __restrict__ W, double E, int k) {
+    const double aE = __dmul_rn(m.a, E);
+    int nodes = 0;
+    double A = 1.0, B = 0.0;
+    int s = 0;
+    for (int i = m.i0; i < k; ++i) {
+        const double Ap = A;
+        step64(aE, __ldg(W + i), A, B);
+        nodes += (A < 0.0) != (Ap < 0.0);
+        if (++s == kRenorm) {
+            s = 0;
+            renorm_pair(A, B);
+        }
+    }
+    double C = 1.0, D = 0.0;
+    s = 0;
+    for (int i = m.i1; i > k; --i) {
+        const double Cp = C;
+        step64(aE, __ldg(W + i), C, D);
+        nodes += (C < 0.0) != (Cp < 0.0);
+        if (++s == kRenorm) {
+            s = 0;
+            renorm_pair(C, D);
+        }
+    }
+    const double Tk = __dsub_rn(aE, __ldg(W + k));
+    const double fk = __dadd_rn(1.0, Tk);
+    const double gk = __fma_rn(-10.0, Tk, 2.0);
+    const double AC = __dmul_rn(A, C);
+    const double num = __fma_rn(gk, AC, -__dmul_rn(fk, __fma_rn(B, C, __dmul_rn(D, A))));
+    nodes += (num < 0.0) != (AC < 0.0);
+    return nodes;
+}
+
+// 1/f for f in [0.4, 4]: FP32 reciprocal refined by two FP64 Newton steps
+// (relative error at the FP64 rounding level).
+__device__ __forceinline__ double recip64(double f) {
+    double r = (double)__frcp_rn((float)f);
+    r = __fma_rn(r, __fma_rn(-f, r, 1.0), r);
+    r = __fma_rn(r, __fma_rn(-f, r, 1.0), r);
+    return r;
+}
+
+}  // namespace epscu

@@ -1,0 +1,694 @@
+// epscu.cu -- host orchestration and C ABI of libepseon_cuda.
+//
+// One context per device: a stream, a growable device arena (block size from
+// HardwareConfig::allocation_block_size, hardware_config.hpp:18), pinned
+// staging buffers, a host-mapped cancel flag polled by the persistent kernels,
+// the autotune cache of the scan kernel and a CUDA graph of the last
+// device-resident solve (replayed when the same buffers are solved again).
+//
+// Solve pipeline (every stage on the context's stream):
+//   prepare -> scan (FP64 | FP32 TMA persistent) -> level set-up + brackets
+//   plain : bisect64 -> norm64 -> write64
+//   fast  : refine32 -> newton64 -> norm64 -> write64
+//   -> gather into the caller's layout.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "epscu.h"
+#include "launch.h"
+
+using namespace epscu;
+
+namespace {
+
+thread_local std::string g_err;
+
+epscu_status fail(epscu_status s, const std::string& msg) {
+    g_err = msg;
+    return s;
+}
+
+#define EPSCU_CU(call)                                                                              \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess)                                                                      \
+            return fail(e_ == cudaErrorMemoryAllocation ? EPSCU_ERR_NOMEM : EPSCU_ERR_CUDA,         \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                        \
+    } while (0)
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+};
+
+constexpr int kStageEvents = 8;
+
+}  // namespace
+
+struct epscu_ctx {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    size_t block = size_t(64) << 20;
+    std::map<std::string, DevBuf> bufs;
+    std::map<std::string, std::pair<void*, size_t>> pinned;
+    volatile int32_t* cancel_host = nullptr;
+    int32_t* cancel_dev = nullptr;
+    cudaEvent_t ev[kStageEvents] = {};
+    // last solve (kept for the adjoint)
+    DevBatch last{};
+    bool have_last = false;
+    int last_method = 0;
+    bool last_psi = false;
+    int64_t* last_offsets_dev = nullptr;
+    int64_t last_total_points = 0;
+    int64_t last_psi_total = 0;
+    epscu_stats stats{};
+    std::map<std::string, ScanShape> tune_cache;
+    // CUDA graph of the last device-resident solve
+    cudaGraphExec_t graph = nullptr;
+    std::string graph_key;
+    std::mutex mu;
+
+    ~epscu_ctx() {
+        cudaSetDevice(device);
+        if (graph) cudaGraphExecDestroy(graph);
+        for (auto& kv : bufs)
+            if (kv.second.p) cudaFree(kv.second.p);
+        for (auto& kv : pinned)
+            if (kv.second.first) cudaFreeHost(kv.second.first);
+        if (cancel_host) cudaFreeHost((void*)cancel_host);
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    // device buffer `name` with at least `bytes` (grown in arena blocks)
+    void* get(const std::string& name, size_t bytes, cudaError_t* err) {
+        DevBuf& b = bufs[name];
+        if (bytes == 0) bytes = 256;
+        if (b.cap >= bytes) return b.p;
+        if (b.p) {
+            cudaStreamSynchronize(stream);
+            cudaFree(b.p);
+            b.p = nullptr;
+            b.cap = 0;
+            if (graph) {  // captured pointers are stale
+                cudaGraphExecDestroy(graph);
+                graph = nullptr;
+                graph_key.clear();
+            }
+        }
+        const size_t blk = block ? block : (size_t(64) << 20);
+        size_t want = bytes < blk ? ((bytes + 4095) & ~size_t(4095)) : ((bytes + blk - 1) / blk) * blk;
+        *err = cudaMalloc(&b.p, want);
+        if (*err != cudaSuccess) {
+            b.p = nullptr;
+            return nullptr;
+        }
+        b.cap = want;
+        return b.p;
+    }
+
+    void* host(const std::string& name, size_t bytes, cudaError_t* err) {
+        auto& h = pinned[name];
+        if (h.second >= bytes && h.first) return h.first;
+        if (h.first) {
+            cudaStreamSynchronize(stream);
+            cudaFreeHost(h.first);
+            if (graph) {
+                cudaGraphExecDestroy(graph);
+                graph = nullptr;
+                graph_key.clear();
+            }
+        }
+        h.first = nullptr;
+        h.second = 0;
+        *err = cudaHostAlloc(&h.first, bytes ? bytes : 64, cudaHostAllocDefault);
+        if (*err != cudaSuccess) {
+            h.first = nullptr;
+            return nullptr;
+        }
+        h.second = bytes;
+        return h.first;
+    }
+};
+
+extern "C" {
+
+int32_t epscu_abi_version(void) { return EPSCU_ABI_VERSION; }
+
+const char* epscu_last_error(void) { return g_err.c_str(); }
+
+epscu_status epscu_device_count(int32_t* count) {
+    if (!count) return fail(EPSCU_ERR_INVALID, "count is NULL");
+    int c = 0;
+    cudaError_t e = cudaGetDeviceCount(&c);
+    if (e != cudaSuccess) {
+        *count = 0;
+        cudaGetLastError();
+        return fail(EPSCU_ERR_CUDA, std::string("cudaGetDeviceCount: ") + cudaGetErrorString(e));
+    }
+    *count = c;
+    return EPSCU_OK;
+}
+
+epscu_status epscu_get_device_info(int32_t ordinal, epscu_device_info* info) {
+    if (!info) return fail(EPSCU_ERR_INVALID, "info is NULL");
+    cudaDeviceProp p;
+    EPSCU_CU(cudaGetDeviceProperties(&p, ordinal));
+    std::memset(info, 0, sizeof(*info));
+    std::strncpy(info->name, p.name, sizeof(info->name) - 1);
+    info->ordinal = ordinal;
+    info->pci_device_id = p.pciDeviceID;
+    info->pci_bus_id = p.pciBusID;
+    info->cc_major = p.major;
+    info->cc_minor = p.minor;
+    info->sm_count = p.multiProcessorCount;
+    info->total_global_mem = (int64_t)p.totalGlobalMem;
+    info->shared_mem_per_block_optin = (int32_t)p.sharedMemPerBlockOptin;
+    info->max_threads_per_block = p.maxThreadsPerBlock;
+    for (int i = 0; i < 3; ++i) {
+        info->max_grid_dim[i] = p.maxGridSize[i];
+        info->max_block_dim[i] = p.maxThreadsDim[i];
+    }
+    info->l2_cache_size = p.l2CacheSize;
+    int dv = 0, rv = 0;
+    cudaDriverGetVersion(&dv);
+    cudaRuntimeGetVersion(&rv);
+    info->driver_version = dv;
+    info->runtime_version = rv;
+    std::memcpy(info->uuid, p.uuid.bytes, 16);
+    return EPSCU_OK;
+}
+
+epscu_status epscu_create(int32_t device_ordinal, epscu_ctx** out) {
+    if (!out) return fail(EPSCU_ERR_INVALID, "ctx out pointer is NULL");
+    *out = nullptr;
+    int count = 0;
+    EPSCU_CU(cudaGetDeviceCount(&count));
+    if (device_ordinal < 0 || device_ordinal >= count)
+        return fail(EPSCU_ERR_INVALID, "device ordinal " + std::to_string(device_ordinal) + " out of range");
+    EPSCU_CU(cudaSetDevice(device_ordinal));
+    auto* c = new epscu_ctx();
+    c->device = device_ordinal;
+    cudaDeviceProp p;
+    cudaError_t e = cudaGetDeviceProperties(&p, device_ordinal);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    void* hc = nullptr;
+    if (e == cudaSuccess) e = cudaHostAlloc(&hc, 64, cudaHostAllocMapped);
+    if (e == cudaSuccess) {
+        c->cancel_host = (volatile int32_t*)hc;
+        *c->cancel_host = 0;
+        e = cudaHostGetDevicePointer((void**)&c->cancel_dev, hc, 0);
+    }
+    for (int i = 0; i < kStageEvents && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
+    if (e != cudaSuccess) {
+        delete c;
+        return fail(EPSCU_ERR_CUDA, std::string("context set-up: ") + cudaGetErrorString(e));
+    }
+    c->sm_count = p.multiProcessorCount;
+    scan32_set_attributes();
+    *out = c;
+    return EPSCU_OK;
+}
+
+epscu_status epscu_destroy(epscu_ctx* ctx) {
+    if (!ctx) return EPSCU_OK;
+    {
+        std::lock_guard<std::mutex> g(ctx->mu);
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
+    }
+    delete ctx;
+    return EPSCU_OK;
+}
+
+epscu_status epscu_set_arena_block(epscu_ctx* ctx, int64_t bytes) {
+    if (!ctx || bytes < 0) return fail(EPSCU_ERR_INVALID, "bad arguments");
+    std::lock_guard<std::mutex> g(ctx->mu);
+    ctx->block = bytes ? (size_t)bytes : (size_t(64) << 20);
+    return EPSCU_OK;
+}
+
+epscu_status epscu_cancel(epscu_ctx* ctx) {
+    if (!ctx) return fail(EPSCU_ERR_INVALID, "ctx is NULL");
+    *ctx->cancel_host = 1;  // no lock: the solve holds it
+    return EPSCU_OK;
+}
+
+epscu_status epscu_last_stats(epscu_ctx* ctx, epscu_stats* stats) {
+    if (!ctx || !stats) return fail(EPSCU_ERR_INVALID, "bad arguments");
+    std::lock_guard<std::mutex> g(ctx->mu);
+    *stats = ctx->stats;
+    return EPSCU_OK;
+}
+
+epscu_status epscu_measure_fma_peaks(epscu_ctx* ctx, double* fp32, double* fp64) {
+    if (!ctx) return fail(EPSCU_ERR_INVALID, "ctx is NULL");
+    std::lock_guard<std::mutex> g(ctx->mu);
+    cudaSetDevice(ctx->device);
+    measure_fma_peaks(ctx->sm_count, fp32, fp64);
+    EPSCU_CU(cudaGetLastError());
+    return EPSCU_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Launch the solve stages of DevBatch b on stream s (capturable).
+void enqueue_pipeline(epscu_ctx* ctx, const DevBatch& b, int method, bool want_psi, const ScanShape& shape,
+                      bool stage_events, cudaStream_t s) {
+    auto rec = [&](int i) {
+        if (stage_events) cudaEventRecord(ctx->ev[i], s);
+    };
+    rec(0);
+    launch_prepare(b, s);
+    rec(1);
+    if (method == EPSCU_METHOD_PLAIN_FP64) launch_scan64(b, s);
+    else launch_scan32(b, shape, ctx->sm_count, s);
+    rec(2);
+    launch_level_setup(b, s);
+    if (method == EPSCU_METHOD_PLAIN_FP64) {
+        launch_bisect64(b, ctx->sm_count, s);
+        rec(3);
+    } else {
+        launch_refine32(b, ctx->sm_count, s);
+        rec(3);
+        launch_newton64(b, ctx->sm_count, s);
+    }
+    launch_norm64(b, method == EPSCU_METHOD_FAST_FP32C ? 1 : 0, ctx->sm_count, s);
+    rec(4);
+    if (want_psi) launch_write64(b, ctx->sm_count, s);
+    rec(5);
+}
+
+std::string shape_key(int n, int n_trial, int64_t total) {
+    return std::to_string(n) + ":" + std::to_string(n_trial) + ":" + std::to_string(total >> 16);
+}
+
+}  // namespace
+
+extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, epscu_result* res,
+                                    const epscu_opts* opts_in) {
+    if (!ctx || !batch || !res) return fail(EPSCU_ERR_INVALID, "NULL argument");
+    epscu_opts opts{};
+    opts.method = EPSCU_METHOD_FAST_FP32C;
+    opts.tol = 1e-12;
+    if (opts_in) opts = *opts_in;
+    if (opts.tol <= 0) opts.tol = 1e-12;
+    std::lock_guard<std::mutex> guard(ctx->mu);
+    cudaSetDevice(ctx->device);
+    const int n = batch->n_potentials;
+    const int cap = res->level_capacity;
+    const int method = opts.method;
+    const bool dev = (opts.flags & EPSCU_MEM_DEVICE) != 0;
+    const bool want_psi = (opts.flags & EPSCU_WANT_PSI) && res->psi && res->psi_capacity > 0;
+    const bool stage_events = (opts.flags & EPSCU_STAGE_TIMING) != 0 || !dev;
+    if (n <= 0) return fail(EPSCU_ERR_INVALID, "n_potentials must be positive");
+    if (cap <= 0) return fail(EPSCU_ERR_INVALID, "level_capacity must be positive");
+    if (method != EPSCU_METHOD_PLAIN_FP64 && method != EPSCU_METHOD_FAST_FP32C)
+        return fail(EPSCU_ERR_INVALID, "unknown method " + std::to_string(method));
+    if (batch->n_trial < 1 || batch->n_trial > (1 << 24)) return fail(EPSCU_ERR_INVALID, "n_trial out of range");
+    if (batch->min_level < 0) return fail(EPSCU_ERR_INVALID, "min_level must be >= 0");
+    if (batch->max_level >= 0 && batch->max_level < batch->min_level)
+        return fail(EPSCU_ERR_INVALID, "max_level < min_level");
+    if (!batch->V || !batch->offsets || !batch->N || !batch->r_min || !batch->r_max || !batch->mu || !batch->e_cap)
+        return fail(EPSCU_ERR_INVALID, "batch array is NULL");
+    if (!res->n_total || !res->n_out || !res->energy || !res->nodes || !res->status)
+        return fail(EPSCU_ERR_INVALID, "result array is NULL");
+    if ((int64_t)n * cap > (int64_t)1 << 30) return fail(EPSCU_ERR_INVALID, "n * level_capacity too large");
+
+    // ---- host-side metadata
+    const int64_t tile = scan32_max_tile();
+    int64_t total_points = 0, total_padded = 0;
+    int32_t max_N = 0;
+    cudaError_t ce = cudaSuccess;
+    auto* hm = (PotMeta*)ctx->host("meta", sizeof(PotMeta) * n, &ce);
+    auto* ho = (int32_t*)ctx->host("order", sizeof(int32_t) * n, &ce);
+    auto* hoff = (int64_t*)ctx->host("offsets", sizeof(int64_t) * n, &ce);
+    if (!hm || !ho || !hoff) return fail(EPSCU_ERR_NOMEM, "pinned staging allocation failed");
+    for (int p = 0; p < n; ++p) {
+        const int32_t N = batch->N[p];
+        const int64_t off = batch->offsets[p];
+        if (N < 5) return fail(EPSCU_ERR_INVALID, "potential " + std::to_string(p) + " has fewer than 5 points");
+        if (off < 0) return fail(EPSCU_ERR_INVALID, "negative offset");
+        if (!(batch->r_max[p] > batch->r_min[p]) || !(batch->mu[p] > 0.0) || !std::isfinite(batch->e_cap[p]))
+            return fail(EPSCU_ERR_INVALID, "potential " + std::to_string(p) + " has a bad grid, mass or energy cap");
+        PotMeta m{};
+        m.r_min = batch->r_min[p];
+        m.r_max = batch->r_max[p];
+        m.mu = batch->mu[p];
+        m.e_cap = batch->e_cap[p];
+        m.off = off;
+        m.offf = total_padded;
+        m.N = N;
+        m.n_trial = batch->n_trial;
+        hm[p] = m;
+        hoff[p] = off;
+        total_points = std::max<int64_t>(total_points, off + N);
+        total_padded += ((N + tile - 1) / tile) * tile;
+        max_N = std::max(max_N, N);
+    }
+    std::vector<int32_t> ord(n);
+    std::iota(ord.begin(), ord.end(), 0);
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return batch->N[a] > batch->N[b]; });
+    std::memcpy(ho, ord.data(), sizeof(int32_t) * n);
+
+    // ---- device buffers
+    cudaStream_t s = opts.stream ? (cudaStream_t)opts.stream : ctx->stream;
+    const int64_t lv = (int64_t)n * cap;
+    DevBatch b{};
+    b.n = n;
+    b.meta = (PotMeta*)ctx->get("meta", sizeof(PotMeta) * n, &ce);
+    b.W64 = (double*)ctx->get("W64", sizeof(double) * total_points, &ce);
+    b.Msuf = (double*)ctx->get("Msuf", sizeof(double) * total_points, &ce);
+    b.Wf2 = method == EPSCU_METHOD_FAST_FP32C ? (float2*)ctx->get("Wf2", sizeof(float2) * total_padded, &ce) : nullptr;
+    b.counts = (int32_t*)ctx->get("counts", sizeof(int32_t) * (size_t)n * batch->n_trial, &ce);
+    b.levels = (LevelWork*)ctx->get("levels", sizeof(LevelWork) * lv, &ce);
+    b.hdr = (Header*)ctx->get("hdr", sizeof(Header), &ce);
+    b.order = (int32_t*)ctx->get("order", sizeof(int32_t) * n, &ce);
+    int64_t* d_off = (int64_t*)ctx->get("offsets", sizeof(int64_t) * n, &ce);
+    if (ce != cudaSuccess || !b.meta || !b.W64 || !b.Msuf || !b.counts || !b.levels || !b.hdr || !b.order || !d_off ||
+        (method == EPSCU_METHOD_FAST_FP32C && !b.Wf2))
+        return fail(EPSCU_ERR_NOMEM, std::string("device arena: ") + cudaGetErrorString(ce));
+    if (dev) {
+        b.V64 = batch->V;
+    } else {
+        double* v = (double*)ctx->get("V64", sizeof(double) * total_points, &ce);
+        if (!v) return fail(EPSCU_ERR_NOMEM, "device arena (V)");
+        b.V64 = v;
+    }
+    b.max_levels = (int32_t)lv;
+    b.level_capacity = cap;
+    b.cancel = ctx->cancel_dev;
+    b.n_trial = batch->n_trial;
+    b.min_level = batch->min_level;
+    b.max_level = batch->max_level;
+    b.max_N = max_N;
+    b.tol = opts.tol;
+    b.psi = nullptr;
+    b.psi_capacity = 0;
+    if (want_psi) {
+        if (dev) {
+            b.psi = res->psi;
+        } else {
+            b.psi = (double*)ctx->get("psi", sizeof(double) * (size_t)res->psi_capacity, &ce);
+            if (!b.psi) return fail(EPSCU_ERR_NOMEM, "device arena (psi)");
+        }
+        b.psi_capacity = res->psi_capacity;
+    }
+    int32_t *o_nt, *o_no, *o_nd, *o_st;
+    double *o_e, *o_err;
+    if (dev) {
+        o_nt = res->n_total;
+        o_no = res->n_out;
+        o_e = res->energy;
+        o_nd = res->nodes;
+        o_st = res->status;
+        o_err = res->err_est;
+    } else {
+        o_nt = (int32_t*)ctx->get("o_nt", sizeof(int32_t) * n, &ce);
+        o_no = (int32_t*)ctx->get("o_no", sizeof(int32_t) * n, &ce);
+        o_e = (double*)ctx->get("o_e", sizeof(double) * lv, &ce);
+        o_nd = (int32_t*)ctx->get("o_nd", sizeof(int32_t) * lv, &ce);
+        o_st = (int32_t*)ctx->get("o_st", sizeof(int32_t) * lv, &ce);
+        o_err = (double*)ctx->get("o_err", sizeof(double) * lv, &ce);
+        if (!o_nt || !o_no || !o_e || !o_nd || !o_st || !o_err) return fail(EPSCU_ERR_NOMEM, "device arena (outputs)");
+    }
+    auto* hh = (Header*)ctx->host("hdr", sizeof(Header), &ce);
+    if (!hh) return fail(EPSCU_ERR_NOMEM, "pinned staging (hdr)");
+    std::memset(hh, 0, sizeof(Header));
+    *ctx->cancel_host = 0;
+
+    // ---- launch shape of the FP32 scan (autotuned per batch shape)
+    ScanShape shape{256, 2048, 3, 0};
+    const std::string skey = shape_key(n, batch->n_trial, total_points);
+    auto it = ctx->tune_cache.find(skey);
+    if (it != ctx->tune_cache.end()) shape = it->second;
+
+    // ---- inputs
+    if (!dev) EPSCU_CU(cudaMemcpyAsync((void*)b.V64, batch->V, sizeof(double) * total_points, cudaMemcpyHostToDevice, s));
+
+    if (method == EPSCU_METHOD_FAST_FP32C && opts.tune && it == ctx->tune_cache.end()) {
+        // time each scan variant on this batch, keep the fastest
+        EPSCU_CU(cudaMemcpyAsync(b.meta, hm, sizeof(PotMeta) * n, cudaMemcpyHostToDevice, s));
+        EPSCU_CU(cudaMemcpyAsync(b.order, ho, sizeof(int32_t) * n, cudaMemcpyHostToDevice, s));
+        EPSCU_CU(cudaMemsetAsync(b.Wf2, 0, sizeof(float2) * total_padded, s));
+        EPSCU_CU(cudaMemsetAsync(b.hdr, 0, sizeof(Header), s));
+        launch_prepare(b, s);
+        const ScanShape cands[] = {{128, 1024, 4, 0}, {128, 2048, 3, 0}, {256, 1024, 4, 0}, {256, 2048, 3, 0},
+                                   {256, 4096, 2, 0}, {512, 1024, 4, 0}, {512, 2048, 3, 0}};
+        float best = 1e30f;
+        for (const ScanShape& c : cands) {
+            EPSCU_CU(cudaMemsetAsync(&b.hdr->queue_scan, 0, sizeof(int32_t), s));
+            EPSCU_CU(cudaEventRecord(ctx->ev[6], s));
+            launch_scan32(b, c, ctx->sm_count, s);
+            EPSCU_CU(cudaEventRecord(ctx->ev[7], s));
+            EPSCU_CU(cudaEventSynchronize(ctx->ev[7]));
+            EPSCU_CU(cudaGetLastError());
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]);
+            if (ms < best) {
+                best = ms;
+                shape = c;
+            }
+        }
+        ctx->tune_cache[skey] = shape;
+    }
+
+    // ---- the pipeline (graph-replayed when the device-resident inputs repeat)
+    const bool use_graph = dev && !stage_events;
+    char keybuf[512];
+    std::snprintf(keybuf, sizeof(keybuf), "%d|%d|%d|%d|%p|%p|%p|%p|%p|%p|%p|%p|%lld|%d|%d|%d|%d|%d|%g|%p", n,
+                  batch->n_trial, batch->min_level, batch->max_level, (const void*)b.V64, (void*)b.psi,
+                  (void*)o_e, (void*)o_nt, (void*)o_no, (void*)o_nd, (void*)o_st, (void*)o_err,
+                  (long long)b.psi_capacity, method, cap, shape.threads, shape.tile, shape.stages, opts.tol,
+                  (void*)s);
+    const std::string gkey = std::string(keybuf) + "|" + std::to_string(total_points);
+
+    auto enqueue_all = [&]() -> cudaError_t {
+        cudaError_t e;
+        if ((e = cudaMemcpyAsync(b.meta, hm, sizeof(PotMeta) * n, cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
+        if ((e = cudaMemcpyAsync(b.order, ho, sizeof(int32_t) * n, cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
+        if ((e = cudaMemcpyAsync(d_off, hoff, sizeof(int64_t) * n, cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
+        if ((e = cudaMemsetAsync(b.hdr, 0, sizeof(Header), s)) != cudaSuccess) return e;
+        if (b.Wf2 && (e = cudaMemsetAsync(b.Wf2, 0, sizeof(float2) * total_padded, s)) != cudaSuccess) return e;
+        enqueue_pipeline(ctx, b, method, want_psi, shape, stage_events, s);
+        launch_gather(b, o_nt, o_no, o_e, o_nd, o_st, o_err, method == EPSCU_METHOD_FAST_FP32C ? 1 : 0, s);
+        if (stage_events) cudaEventRecord(ctx->ev[6], s);
+        return cudaGetLastError();
+    };
+
+    if (use_graph) {
+        if (!ctx->graph || ctx->graph_key != gkey) {
+            if (ctx->graph) {
+                cudaGraphExecDestroy(ctx->graph);
+                ctx->graph = nullptr;
+            }
+            cudaGraph_t g = nullptr;
+            EPSCU_CU(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            cudaError_t e = enqueue_all();
+            cudaError_t e2 = cudaStreamEndCapture(s, &g);
+            if (e != cudaSuccess || e2 != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                return fail(EPSCU_ERR_CUDA, std::string("graph capture: ") +
+                                                cudaGetErrorString(e != cudaSuccess ? e : e2));
+            }
+            e = cudaGraphInstantiate(&ctx->graph, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) {
+                ctx->graph = nullptr;
+                return fail(EPSCU_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+            }
+            ctx->graph_key = gkey;
+        }
+        EPSCU_CU(cudaEventRecord(ctx->ev[0], s));
+        EPSCU_CU(cudaGraphLaunch(ctx->graph, s));
+        EPSCU_CU(cudaEventRecord(ctx->ev[6], s));
+    } else {
+        EPSCU_CU(enqueue_all());
+    }
+
+    // ---- outputs back
+    if (!dev) {
+        EPSCU_CU(cudaMemcpyAsync(res->n_total, o_nt, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
+        EPSCU_CU(cudaMemcpyAsync(res->n_out, o_no, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
+        EPSCU_CU(cudaMemcpyAsync(res->energy, o_e, sizeof(double) * lv, cudaMemcpyDeviceToHost, s));
+        EPSCU_CU(cudaMemcpyAsync(res->nodes, o_nd, sizeof(int32_t) * lv, cudaMemcpyDeviceToHost, s));
+        EPSCU_CU(cudaMemcpyAsync(res->status, o_st, sizeof(int32_t) * lv, cudaMemcpyDeviceToHost, s));
+        if (res->err_est)
+            EPSCU_CU(cudaMemcpyAsync(res->err_est, o_err, sizeof(double) * lv, cudaMemcpyDeviceToHost, s));
+    }
+    EPSCU_CU(cudaMemcpyAsync(hm, b.meta, sizeof(PotMeta) * n, cudaMemcpyDeviceToHost, s));
+    EPSCU_CU(cudaMemcpyAsync(hh, b.hdr, sizeof(Header), cudaMemcpyDeviceToHost, s));
+    EPSCU_CU(cudaStreamSynchronize(s));
+    EPSCU_CU(cudaGetLastError());
+
+    // psi offsets / size
+    int64_t psi_total = 0;
+    for (int p = 0; p < n; ++p) {
+        if (res->psi_offsets) res->psi_offsets[p] = hm[p].psi_off;
+        psi_total = std::max<int64_t>(psi_total, hm[p].psi_off + (int64_t)hm[p].n_out * hm[p].N);
+    }
+    res->psi_required = psi_total;
+    if (want_psi && !dev && hh->error == 0 && psi_total > 0)
+        EPSCU_CU(cudaMemcpy(res->psi, b.psi, sizeof(double) * psi_total, cudaMemcpyDeviceToHost));
+
+    // stats
+    epscu_stats st{};
+    float ms = 0.f;
+    if (stage_events) {
+        auto el = [&](int a, int c) {
+            float x = 0.f;
+            cudaEventElapsedTime(&x, ctx->ev[a], ctx->ev[c]);
+            return x;
+        };
+        st.ms_prepare = el(0, 1);
+        st.ms_scan = el(1, 2);
+        if (method == EPSCU_METHOD_PLAIN_FP64) {
+            st.ms_refine32 = 0.f;
+            st.ms_polish64 = el(2, 3) + el(3, 4);
+        } else {
+            st.ms_refine32 = el(2, 3);
+            st.ms_polish64 = el(3, 4);
+        }
+        st.ms_write = el(4, 5);
+        st.ms_total = el(0, 6);
+    } else {
+        cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[6]);
+        st.ms_total = ms;
+    }
+    int64_t scan_pts = 0, lvl_pts = 0;
+    int64_t nlev = 0;
+    for (int p = 0; p < n; ++p) {
+        const int64_t interior = std::max(0, hm[p].i1 - hm[p].i0);
+        scan_pts += interior * batch->n_trial;
+        lvl_pts += interior * hm[p].n_out;
+        nlev += hm[p].n_out;
+    }
+    st.scan_point_updates = scan_pts;
+    st.n_levels = nlev;
+    st.fallbacks = hh->fallbacks;
+    st.psi_bytes = want_psi ? psi_total * 8 : 0;
+    st.kernel_launches = 7 + (want_psi ? 1 : 0) + (method == EPSCU_METHOD_FAST_FP32C ? 1 : 0);
+    if (method == EPSCU_METHOD_PLAIN_FP64) {
+        st.refine_point_updates = 0;
+        int64_t bis = 0;
+        for (int p = 0; p < n; ++p) bis += (int64_t)std::max(0, hm[p].i1 - hm[p].i0) * hm[p].n_out * hm[p].n_bisect;
+        st.fp64_point_updates = scan_pts + bis + lvl_pts * (want_psi ? 2 : 1);
+    } else {
+        st.refine_point_updates = -1;  // data-dependent iteration counts
+        st.fp64_point_updates = lvl_pts * (want_psi ? 3 : 2);
+    }
+    ctx->stats = st;
+
+    // keep for the adjoint
+    ctx->last = b;
+    ctx->have_last = true;
+    ctx->last_method = method;
+    ctx->last_psi = want_psi && hh->error == 0;
+    ctx->last_offsets_dev = d_off;
+    ctx->last_total_points = total_points;
+    ctx->last_psi_total = psi_total;
+
+    if (hh->error == EPSCU_ERR_CAPACITY || (want_psi && psi_total > res->psi_capacity))
+        return fail(EPSCU_ERR_CAPACITY, "psi buffer too small: " + std::to_string(psi_total) + " doubles required");
+    if (hh->error) return fail(hh->error, "device-side error " + std::to_string(hh->error));
+    if (*ctx->cancel_host) return fail(EPSCU_ERR_CANCELLED, "solve cancelled");
+    return EPSCU_OK;
+}
+
+extern "C" epscu_status epscu_adjoint(epscu_ctx* ctx, const double* dL_dE, double* dL_dV, int32_t recompute,
+                                      const epscu_opts* opts_in) {
+    if (!ctx || !dL_dE || !dL_dV) return fail(EPSCU_ERR_INVALID, "NULL argument");
+    epscu_opts opts{};
+    if (opts_in) opts = *opts_in;
+    std::lock_guard<std::mutex> guard(ctx->mu);
+    cudaSetDevice(ctx->device);
+    if (!ctx->have_last) return fail(EPSCU_ERR_INVALID, "no solve to differentiate on this context");
+    DevBatch b = ctx->last;
+    cudaStream_t s = opts.stream ? (cudaStream_t)opts.stream : ctx->stream;
+    cudaError_t ce = cudaSuccess;
+    if (!ctx->last_psi) {
+        if (!recompute) return fail(EPSCU_ERR_INVALID, "last solve kept no wavefunctions; pass recompute=1");
+        // recompute psi of the last solve into the arena
+        double* psi = (double*)ctx->get("psi_adj", sizeof(double) * (size_t)std::max<int64_t>(1, ctx->last_psi_total), &ce);
+        if (!psi) return fail(EPSCU_ERR_NOMEM, "device arena (recomputed psi)");
+        b.psi = psi;
+        b.psi_capacity = ctx->last_psi_total;
+        launch_write64(b, ctx->sm_count, s);
+    }
+    const bool dev = (opts.flags & EPSCU_MEM_DEVICE) != 0;
+    const int64_t lv = (int64_t)b.n * b.level_capacity;
+    const double* gE = dL_dE;
+    double* gV = dL_dV;
+    if (!dev) {
+        double* d_gE = (double*)ctx->get("adj_gE", sizeof(double) * lv, &ce);
+        double* d_gV = (double*)ctx->get("adj_gV", sizeof(double) * ctx->last_total_points, &ce);
+        if (!d_gE || !d_gV) return fail(EPSCU_ERR_NOMEM, "device arena (adjoint)");
+        EPSCU_CU(cudaMemcpyAsync(d_gE, dL_dE, sizeof(double) * lv, cudaMemcpyHostToDevice, s));
+        EPSCU_CU(cudaMemsetAsync(d_gV, 0, sizeof(double) * ctx->last_total_points, s));
+        gE = d_gE;
+        gV = d_gV;
+    }
+    launch_adjoint(b, gE, gV, ctx->last_total_points, ctx->last_offsets_dev, recompute, ctx->sm_count, s);
+    EPSCU_CU(cudaGetLastError());
+    if (!dev) EPSCU_CU(cudaMemcpyAsync(dL_dV, gV, sizeof(double) * ctx->last_total_points, cudaMemcpyDeviceToHost, s));
+    EPSCU_CU(cudaStreamSynchronize(s));
+    return EPSCU_OK;
+}
+
+extern "C" epscu_status epscu_tabulate(epscu_ctx* ctx, int32_t n, const int32_t* kind, const double* params,
+                                       const int64_t* offsets, const int32_t* N, const double* r_min,
+                                       const double* r_max, int32_t n_knots, double* V, const epscu_opts* opts_in) {
+    if (!ctx || n <= 0 || !kind || !params || !offsets || !N || !r_min || !r_max || !V)
+        return fail(EPSCU_ERR_INVALID, "bad arguments");
+    if (n_knots < 4) n_knots = 1024;
+    epscu_opts opts{};
+    if (opts_in) opts = *opts_in;
+    std::lock_guard<std::mutex> guard(ctx->mu);
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = opts.stream ? (cudaStream_t)opts.stream : ctx->stream;
+    const bool dev = (opts.flags & EPSCU_MEM_DEVICE) != 0;
+    int64_t total = 0;
+    // host copies of the per-potential arrays (always host-side per the ABI)
+    for (int p = 0; p < n; ++p) {
+        if (N[p] < 2) return fail(EPSCU_ERR_INVALID, "grid with fewer than 2 points");
+        total = std::max<int64_t>(total, offsets[p] + N[p]);
+    }
+    cudaError_t ce = cudaSuccess;
+    auto* d_kind = (int32_t*)ctx->get("tab_kind", sizeof(int32_t) * n, &ce);
+    auto* d_par = (double*)ctx->get("tab_par", sizeof(double) * 12 * n, &ce);
+    auto* d_off = (int64_t*)ctx->get("tab_off", sizeof(int64_t) * n, &ce);
+    auto* d_N = (int32_t*)ctx->get("tab_N", sizeof(int32_t) * n, &ce);
+    auto* d_r0 = (double*)ctx->get("tab_r0", sizeof(double) * n, &ce);
+    auto* d_r1 = (double*)ctx->get("tab_r1", sizeof(double) * n, &ce);
+    auto* d_scr = (double*)ctx->get("tab_scratch", sizeof(double) * 3 * (size_t)n_knots * n, &ce);
+    if (!d_kind || !d_par || !d_off || !d_N || !d_r0 || !d_r1 || !d_scr) return fail(EPSCU_ERR_NOMEM, "device arena");
+    EPSCU_CU(cudaMemcpyAsync(d_kind, kind, sizeof(int32_t) * n, cudaMemcpyHostToDevice, s));
+    EPSCU_CU(cudaMemcpyAsync(d_par, params, sizeof(double) * 12 * n, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+    EPSCU_CU(cudaMemcpyAsync(d_off, offsets, sizeof(int64_t) * n, cudaMemcpyHostToDevice, s));
+    EPSCU_CU(cudaMemcpyAsync(d_N, N, sizeof(int32_t) * n, cudaMemcpyHostToDevice, s));
+    EPSCU_CU(cudaMemcpyAsync(d_r0, r_min, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    EPSCU_CU(cudaMemcpyAsync(d_r1, r_max, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    double* out = V;
+    if (!dev) {
+        out = (double*)ctx->get("tab_V", sizeof(double) * total, &ce);
+        if (!out) return fail(EPSCU_ERR_NOMEM, "device arena (V)");
+    }
+    launch_tabulate(n, d_kind, d_par, d_off, d_N, d_r0, d_r1, n_knots, d_scr, out, s);
+    EPSCU_CU(cudaGetLastError());
+    if (!dev) EPSCU_CU(cudaMemcpyAsync(V, out, sizeof(double) * total, cudaMemcpyDeviceToHost, s));
+    EPSCU_CU(cudaStreamSynchronize(s));
+    return EPSCU_OK;
+}

@@ -1,0 +1,69 @@
+// launch.h -- host-side launchers of the libepseon_cuda kernels (one per
+// translation unit), called by the orchestration in epscu.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace epscu {
+
+struct DevBatch {
+    int32_t n;                 // potentials
+    PotMeta* meta;             // [n]
+    const double* V64;         // concatenated potentials
+    double* W64;               // a V (FP64)
+    double* Msuf;              // suffix minima of V on i0..i1
+    float2* Wf2;               // a V as (hi, lo) floats, tile-aligned per potential
+    int32_t* counts;           // [n * n_trial]
+    LevelWork* levels;         // [max_levels]
+    int32_t max_levels;        // capacity of levels (n * level_capacity)
+    int32_t level_capacity;    // slots per potential
+    Header* hdr;
+    int32_t* order;            // [n] potentials by decreasing cost
+    double* psi;               // compact wavefunctions or nullptr
+    int64_t psi_capacity;
+    volatile int32_t* cancel;  // host-mapped cancel flag (device pointer) or nullptr
+    int32_t n_trial;
+    int32_t min_level, max_level;
+    int32_t max_N;             // longest grid of the batch
+    double tol;
+};
+
+// prepare.cu
+void launch_prepare(const DevBatch& b, cudaStream_t s);
+void launch_level_setup(const DevBatch& b, cudaStream_t s);
+void launch_tabulate(int32_t n, const int32_t* kind, const double* params, const int64_t* offsets,
+                     const int32_t* N, const double* r_min, const double* r_max, int32_t n_knots,
+                     double* knot_scratch, double* V, cudaStream_t s);
+
+// scan.cu
+void launch_scan64(const DevBatch& b, cudaStream_t s);
+struct ScanShape {
+    int threads;      // threads per CTA (energies per CTA = threads)
+    int tile;         // floats2 per TMA stage
+    int stages;
+    int ctas_per_sm;  // persistent grid = sm_count * ctas_per_sm
+};
+void launch_scan32(const DevBatch& b, const ScanShape& shape, int sm_count, cudaStream_t s);
+int scan32_max_tile();
+void scan32_set_attributes();
+
+// levels.cu
+void launch_bisect64(const DevBatch& b, int sm_count, cudaStream_t s);
+void launch_refine32(const DevBatch& b, int sm_count, cudaStream_t s);
+void launch_newton64(const DevBatch& b, int sm_count, cudaStream_t s);
+void launch_norm64(const DevBatch& b, int use_k, int sm_count, cudaStream_t s);
+void launch_write64(const DevBatch& b, int sm_count, cudaStream_t s);
+void launch_gather(const DevBatch& b, int32_t* n_total, int32_t* n_out, double* energy, int32_t* nodes,
+                   int32_t* status, double* err_est, int apply_dE, cudaStream_t s);
+
+// adjoint.cu
+void launch_adjoint(const DevBatch& b, const double* dL_dE, double* dL_dV, int64_t total_points,
+                    const int64_t* offsets_dev, int recompute, int sm_count, cudaStream_t s);
+
+// peaks.cu
+void measure_fma_peaks(int sm_count, double* fp32_tflops, double* fp64_tflops);
+
+}  // namespace epscu

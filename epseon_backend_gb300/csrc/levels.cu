@@ -1,0 +1,509 @@
+// levels.cu -- per-level refinement, normalisation and write-back.
+//
+// Every kernel here is persistent (grid = SMs x resident CTAs) and walks the
+// level slots written by the bracket kernel; the number of slots is read from
+// device memory, so the whole solve can be captured in one CUDA graph.
+//
+//  bisect64 : plain method, FP64 bisection on the twisted Sturm count with the
+//             match index k(E) (outer classical turning point), n_bisect halvings
+//             of the scan bracket -- identical arithmetic to the oracle.
+//  refine32 : fast method, safeguarded Cooley-Newton iteration in the FP32
+//             difference form (count + matching residual + norm per pass).
+//  newton64 : fast method, one FP64 Cooley correction from the FP32 energy.
+//  norm64   : FP64 Cooley pass that also fixes the normalisation constants
+//             (sum psi^2 h = 1, psi > 0 next to the inner wall) and the node
+//             count reported for the level.
+//  write64  : recomputes the FP64 recurrence and writes psi.
+//  gather   : level slots -> the caller's [potential x capacity] layout; the
+//             fast method reports E + dE of the last FP64 pass, the plain
+//             method the bisection midpoint itself.
+//
+// Scale handling: the divide-free state after step i is s_{i+1} (u_{i+1}, u_i)
+// with s_{i+1} = f_{i0} ... f_i, so psi_i = u_i / f_i = A_i / s_{i+1}.  Sums
+// of psi^2 use S_{i+1} = f_i^2 S_i + A_i^2 (no division); the write pass
+// carries q_i = 1 / s_i with a refined reciprocal of f_i.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "launch.h"
+
+namespace epscu {
+
+namespace {
+
+constexpr int kLevelThreads = 128;
+
+__device__ __forceinline__ bool cancelled(const DevBatch& b) { return b.cancel && *b.cancel; }
+
+// match points stay off the two boundary points (both sides non-empty)
+__device__ __forceinline__ int clamp_inner(const PotMeta& m, int k) { return max(m.i0 + 1, min(k, m.i1 - 1)); }
+
+// move the match point to the peak of |psi| when |psi| there is > 4x |psi_k|
+constexpr int kPeakLog2 = 3;
+
+// ------------------------------------------------------------------ FP64 pass
+
+struct Side64 {
+    double A, B, S, q;  // state, psi^2 sum, 1/s (TRACK only)
+    int eA, eQ;         // exponents removed from A/B and from q
+    int nodes;
+    int peak_L, peak_i;  // TRACK: largest log2 |psi-hat| seen at a renormalisation point, and where
+};
+
+template <bool TRACK, bool WRITE>
+__device__ __forceinline__ void side64(const double* __restrict__ W, double aE, int from, int to, int dir, Side64& st,
+                                       double* __restrict__ out, double L, int Xk) {
+    st.A = 1.0;
+    st.B = 0.0;
+    st.S = 0.0;
+    st.q = 1.0;
+    st.eA = 0;
+    st.eQ = 0;
+    st.nodes = 0;
+    st.peak_L = -1 << 30;
+    st.peak_i = from;
+    int s = 0;
+    double F = 0.0;
+    if (WRITE) F = L * ldexp(1.0, min(1000, max(-1100, -Xk)));
+    for (int i = from; i != to; i += dir) {
+        const double T = __dsub_rn(aE, __ldg(W + i));
+        const double f = __dadd_rn(1.0, T);
+        if (TRACK) {
+            const double qn = st.q * recip64(f);
+            if (WRITE) out[i] = st.A * qn * F;
+            st.q = qn;
+        }
+        if (!WRITE) st.S = __fma_rn(f * f, st.S, st.A * st.A);
+        const double g = __fma_rn(-10.0, T, 2.0);
+        const double An = __fma_rn(g, st.A, -__dmul_rn(f, st.B));
+        st.B = __dmul_rn(f, st.A);
+        st.nodes += (An < 0.0) != (st.A < 0.0);
+        st.A = An;
+        if (++s == kRenorm) {
+            s = 0;
+            const int e = renorm_pair(st.A, st.B);
+            st.eA += e;
+            if (!WRITE && e) st.S *= pow2(-2 * e);
+            if (TRACK) {
+                const int eq = exp_of(st.q);
+                st.q *= pow2(-eq);
+                st.eQ += eq;
+                if (!WRITE) {
+                    const double mag = fabs(st.A * st.q);
+                    if (mag > 0.0) {
+                        const int L = exp_of(mag) + st.eA + st.eQ;
+                        if (L > st.peak_L) {
+                            st.peak_L = L;
+                            st.peak_i = i;
+                        }
+                    }
+                }
+            }
+            if (WRITE) F = L * ldexp(1.0, min(1000, max(-1100, st.eA + st.eQ - Xk)));
+        }
+    }
+}
+
+struct Pass64 {
+    double dE, gamma, sum;
+    double pk_out, pk_in;  // psi-hat at k from each side (TRACK)
+    int ex_out, ex_in;
+    int nodes;
+    int peak_i;       // TRACK: where |psi| peaks (sampled every kRenorm points)
+    int peak_log2;    // TRACK: log2 of that peak over |psi| at k
+};
+
+template <bool TRACK>
+__device__ Pass64 cooley64(const PotMeta& m, const double* __restrict__ W, double E, int k) {
+    const double aE = __dmul_rn(m.a, E);
+    Side64 o, in;
+    side64<TRACK, false>(W, aE, m.i0, k, +1, o, nullptr, 0.0, 0);
+    side64<TRACK, false>(W, aE, m.i1, k, -1, in, nullptr, 0.0, 0);
+    const double Tk = __dsub_rn(aE, __ldg(W + k));
+    const double fk = __dadd_rn(1.0, Tk);
+    const double gk = __fma_rn(-10.0, Tk, 2.0);
+    Pass64 r;
+    const double fk2 = fk * fk;
+    r.sum = fk2 * (o.S / (o.A * o.A) + in.S / (in.A * in.A)) + 1.0;
+    r.gamma = gk / fk - o.B / o.A - in.B / in.A;
+    r.dE = r.gamma * fk2 / (12.0 * m.a * r.sum);
+    r.nodes = o.nodes + in.nodes;
+    if (TRACK) {
+        const double rk = recip64(fk);
+        r.pk_out = o.A * o.q * rk;
+        r.pk_in = in.A * in.q * rk;
+        r.ex_out = o.eA + o.eQ;
+        r.ex_in = in.eA + in.eQ;
+        const int Lo = (r.pk_out != 0.0 ? exp_of(fabs(r.pk_out)) : -1000) + r.ex_out;
+        const int Li = (r.pk_in != 0.0 ? exp_of(fabs(r.pk_in)) : -1000) + r.ex_in;
+        const int po = o.peak_L - Lo, pi = in.peak_L - Li;
+        r.peak_log2 = max(po, pi);
+        r.peak_i = po >= pi ? o.peak_i : in.peak_i;
+    } else {
+        r.pk_out = r.pk_in = 0.0;
+        r.ex_out = r.ex_in = 0;
+        r.peak_log2 = 0;
+        r.peak_i = k;
+    }
+    return r;
+}
+
+// Plain FP64 count pass with the twisted pivot: gamma_k and the stitched
+// node count (no sums), for the Newton step of the fast method.
+__device__ __forceinline__ double gamma64(const PotMeta& m, const double* __restrict__ W, double E, int k, int& nodes) {
+    const double aE = __dmul_rn(m.a, E);
+    double A = 1.0, B = 0.0, C = 1.0, D = 0.0;
+    nodes = 0;
+    int s = 0;
+    for (int i = m.i0; i < k; ++i) {
+        const double Ap = A;
+        step64(aE, __ldg(W + i), A, B);
+        nodes += (A < 0.0) != (Ap < 0.0);
+        if (++s == kRenorm) {
+            s = 0;
+            renorm_pair(A, B);
+        }
+    }
+    s = 0;
+    for (int i = m.i1; i > k; --i) {
+        const double Cp = C;
+        step64(aE, __ldg(W + i), C, D);
+        nodes += (C < 0.0) != (Cp < 0.0);
+        if (++s == kRenorm) {
+            s = 0;
+            renorm_pair(C, D);
+        }
+    }
+    const double Tk = __dsub_rn(aE, __ldg(W + k));
+    const double fk = __dadd_rn(1.0, Tk);
+    const double gk = __fma_rn(-10.0, Tk, 2.0);
+    return gk / fk - B / A - D / C;
+}
+
+// ----------------------------------------------------------------- kernels
+
+__global__ void __launch_bounds__(kLevelThreads) bisect64_kernel(DevBatch b) {
+    const int total = b.hdr->total_levels;
+    for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < total; slot += gridDim.x * blockDim.x) {
+        LevelWork w = b.levels[slot];
+        if (w.status & EPSCU_STATUS_NOTFOUND) continue;
+        if (cancelled(b)) {
+            b.levels[slot].status = w.status | EPSCU_STATUS_CANCELLED;
+            continue;
+        }
+        const PotMeta m = b.meta[w.p];
+        const double* W = b.W64 + m.off;
+        double lo = w.lo, hi = w.hi;
+        for (int it = 0; it < m.n_bisect; ++it) {
+            const double mid = __dmul_rn(0.5, __dadd_rn(lo, hi));
+            if (count64(m, W, mid, match_index(m, b.Msuf, mid)) > w.v) hi = mid;
+            else lo = mid;
+        }
+        w.lo = lo;
+        w.hi = hi;
+        w.E = __dmul_rn(0.5, __dadd_rn(lo, hi));
+        w.iters = m.n_bisect;
+        b.levels[slot] = w;
+    }
+}
+
+// FP32 Cooley pass in the difference form; returns dE (FP64), count, nodes,
+// sum psi~^2 and where |psi| peaks (sampled every 16 points, u = f s psi used
+// as the proxy: the scale s barely moves against exponential growth).
+struct Pass32 {
+    double dE, sum;
+    int count, nodes;
+    int peak_i, peak_log2;
+};
+
+__device__ __forceinline__ Pass32 cooley32(const PotMeta& m, const float2* __restrict__ Wf, const double* __restrict__ W64,
+                                           double E, int k) {
+    const double aE = __dmul_rn(m.a, E);
+    const float aEh = __double2float_rn(aE);
+    const float aEl = __double2float_rn(aE - (double)aEh);
+    float Ao = 1.f, Do = 1.f, So = 0.f, Ai = 1.f, Di = 1.f, Si = 0.f;
+    int Lk[2] = {0, 0}, Lpk[2] = {-(1 << 30), -(1 << 30)}, ipk[2] = {m.i0, m.i1};
+    int nodes = 0;
+    for (int side = 0; side < 2; ++side) {
+        float A = 1.0f, D = 1.0f, S = 0.0f;
+        const int from = side == 0 ? m.i0 : m.i1;
+        const int to = k;
+        const int dir = side == 0 ? 1 : -1;
+        int s = 0, ecum = 0;
+        for (int i = from; i != to; i += dir) {
+            const float2 w = __ldg(Wf + i);
+            const float T = (aEh - w.x) + (aEl - w.y);
+            const float f = 1.0f + T;
+            S = fmaf(f * f, S, A * A);
+            const float X = fmaf(-12.0f, A, D);
+            D = fmaf(T, X, D);
+            const float An = A + fmaf(T, A, D);
+            nodes += (__float_as_uint(An) ^ __float_as_uint(A)) >> 31;
+            A = An;
+            if (++s == 16) {
+                s = 0;
+                const float mm = fmaxf(fabsf(A), fabsf(D));
+                const int e = ((__float_as_int(mm) >> 23) & 0xff) - 126;
+                if (mm > 0.0f && e > -60 && e < 60) {
+                    const float sc = __int_as_float((127 - e) << 23);
+                    A *= sc;
+                    D *= sc;
+                    S *= sc * sc;
+                    ecum += e;
+                }
+                const int L = ecum + ((__float_as_int(fabsf(A)) >> 23) & 0xff);
+                if (A != 0.0f && L > Lpk[side]) {
+                    Lpk[side] = L;
+                    ipk[side] = i;
+                }
+            }
+        }
+        Lk[side] = ecum + (A != 0.0f ? ((__float_as_int(fabsf(A)) >> 23) & 0xff) : -1000);
+        if (side == 0) {
+            Ao = A;
+            Do = D;
+            So = S;
+        } else {
+            Ai = A;
+            Di = D;
+            Si = S;
+        }
+    }
+    const double Tk = aE - W64[k];
+    const double fk = 1.0 + Tk;
+    const double uA = Ao, vC = Ai;
+    // gamma_k = -12 T_k / f_k + D_o / u_k + D_i / v_k   (no cancellation)
+    const double gamma = -12.0 * Tk / fk + (double)Do / uA + (double)Di / vC;
+    const double fk2 = fk * fk;
+    Pass32 r;
+    r.sum = fk2 * ((double)So / (uA * uA) + (double)Si / (vC * vC)) + 1.0;
+    r.dE = gamma * fk2 / (12.0 * m.a * r.sum);
+    r.nodes = nodes;
+    r.count = nodes + (gamma < 0.0 ? 1 : 0);
+    const int po = Lpk[0] - Lk[0], pi = Lpk[1] - Lk[1];
+    r.peak_log2 = max(po, pi);
+    r.peak_i = po >= pi ? ipk[0] : ipk[1];
+    return r;
+}
+
+// Safeguarded Cooley-Newton in FP32.  The match point is the outer turning
+// point unless |psi| stitched there peaks > 4x higher elsewhere (an inner-
+// well level of a double well), then that peak.  Every pass updates the count
+// bracket; a small Newton step is confirmed by a count on the far side of the
+// predicted root, otherwise the level continues by bisection.
+constexpr double kTol32 = 2e-9;
+
+__global__ void __launch_bounds__(kLevelThreads) refine32_kernel(DevBatch b) {
+    const int total = b.hdr->total_levels;
+    for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < total; slot += gridDim.x * blockDim.x) {
+        LevelWork w = b.levels[slot];
+        if (w.status & EPSCU_STATUS_NOTFOUND) continue;
+        if (cancelled(b)) {
+            b.levels[slot].status = w.status | EPSCU_STATUS_CANCELLED;
+            continue;
+        }
+        const PotMeta m = b.meta[w.p];
+        const float2* Wf = b.Wf2 + m.offf;
+        const double* W64 = b.W64 + m.off;
+        double lo = w.lo, hi = w.hi, E = w.E;
+        int k = clamp_inner(m, match_index(m, b.Msuf, E));
+        bool k_fixed = false, bisect = false, confirming = false, done = false;
+        double E_star = E, sum = 1.0;
+        int it = 0;
+        for (; it < 48; ++it) {
+            const Pass32 r = cooley32(m, Wf, W64, E, k);
+            if (r.count > w.v) hi = E;
+            else lo = E;
+            sum = r.sum;
+            if (!k_fixed) {
+                k_fixed = true;
+                if (r.peak_log2 >= kPeakLog2) {  // redo at the same energy with the better match point
+                    k = clamp_inner(m, r.peak_i);
+                    continue;
+                }
+            }
+            if (confirming) {
+                confirming = false;
+                if (hi - lo <= 3.0 * kTol32 + 1e-15 && E_star >= lo && E_star <= hi) {
+                    done = true;
+                    break;
+                }
+                bisect = true;  // the predicted root was not confirmed
+            }
+            if (hi - lo <= 2.0 * kTol32) {
+                E_star = 0.5 * (lo + hi);
+                done = true;
+                break;
+            }
+            double En;
+            if (!bisect) {
+                En = E + r.dE;
+                if (!(En > lo && En < hi) || !isfinite(En)) {
+                    En = 0.5 * (lo + hi);
+                } else if (fabs(r.dE) <= kTol32) {
+                    E_star = En;
+                    En = En + (r.dE >= 0.0 ? kTol32 : -kTol32);
+                    if (En <= lo || En >= hi) En = 0.5 * (E_star + (r.dE >= 0.0 ? hi : lo));
+                    confirming = true;
+                }
+            } else {
+                En = 0.5 * (lo + hi);
+            }
+            E = En;
+        }
+        if (!done) {
+            w.status |= EPSCU_STATUS_MAXITER;
+            E_star = 0.5 * (lo + hi);
+        }
+        w.lo = lo;
+        w.hi = hi;
+        w.E = E_star;
+        w.k = k;
+        w.norm_k_in = sum;  // sum psi~^2 of the last pass, the Newton denominator of newton64
+        w.iters = it;
+        b.levels[slot] = w;
+    }
+}
+
+// One FP64 Cooley correction from the FP32 energy at the FP32 match point,
+// with the FP32 sum psi~^2 as the Newton denominator (it only scales the step).
+// A correction inconsistent with the FP32 bracket or a stitched solution
+// with the wrong node count falls back to FP64 bisection on the scan bracket
+// widened by one trial spacing.
+__global__ void __launch_bounds__(kLevelThreads) newton64_kernel(DevBatch b) {
+    const int total = b.hdr->total_levels;
+    for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < total; slot += gridDim.x * blockDim.x) {
+        LevelWork w = b.levels[slot];
+        if (w.status & (EPSCU_STATUS_NOTFOUND | EPSCU_STATUS_CANCELLED)) continue;
+        const PotMeta m = b.meta[w.p];
+        const double* W = b.W64 + m.off;
+        int nodes = 0;
+        const double gamma = gamma64(m, W, w.E, w.k, nodes);
+        const double Tk = __dsub_rn(__dmul_rn(m.a, w.E), __ldg(W + w.k));
+        const double fk = 1.0 + Tk;
+        const double dE = gamma * fk * fk / (12.0 * m.a * w.norm_k_in);
+        const double En = w.E + dE;
+        const double slack = 4.0 * (w.hi - w.lo) + 1e-8;
+        if (nodes != w.v || !(fabs(dE) <= slack) || !isfinite(En)) {
+            const PotMeta mm = m;
+            const int j = (int)floor((w.E - mm.e_lo) / mm.delta);
+            double lo = fmax(mm.e_lo, mm.e_lo + (j - 1) * mm.delta), hi = fmin(mm.e_cap, mm.e_lo + (j + 2) * mm.delta);
+            atomicAdd(&b.hdr->fallbacks, 1);
+            for (int itb = 0; itb < mm.n_bisect + 3; ++itb) {
+                const double mid = __dmul_rn(0.5, __dadd_rn(lo, hi));
+                if (count64(mm, W, mid, w.k) > w.v) hi = mid;
+                else lo = mid;
+            }
+            w.E = __dmul_rn(0.5, __dadd_rn(lo, hi));
+        } else {
+            w.E = En;
+        }
+        b.levels[slot] = w;
+    }
+}
+
+// use_k: keep the match point chosen by the FP32 refinement (fast method);
+// otherwise the outer turning point, moved to the peak of |psi| when the
+// solution stitched there peaks more than 4x higher elsewhere (as the oracle).
+__global__ void __launch_bounds__(kLevelThreads) norm64_kernel(DevBatch b, int use_k) {
+    const int total = b.hdr->total_levels;
+    for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < total; slot += gridDim.x * blockDim.x) {
+        LevelWork w = b.levels[slot];
+        if (w.status & (EPSCU_STATUS_NOTFOUND | EPSCU_STATUS_CANCELLED)) continue;
+        const PotMeta m = b.meta[w.p];
+        int k = use_k ? w.k : clamp_inner(m, match_index(m, b.Msuf, w.E));
+        Pass64 r = cooley64<true>(m, b.W64 + m.off, w.E, k);
+        if (!use_k && r.peak_log2 >= kPeakLog2) {
+            k = clamp_inner(m, r.peak_i);
+            r = cooley64<true>(m, b.W64 + m.off, w.E, k);
+        }
+        double ck = 1.0 / sqrt(m.h * r.sum);
+        if (r.pk_out < 0.0) ck = -ck;  // psi > 0 next to the inner wall
+        w.k = k;
+        w.ck = ck;
+        w.norm_k_out = ck / r.pk_out;
+        w.norm_k_in = ck / r.pk_in;
+        w.ex_out = r.ex_out;
+        w.ex_in = r.ex_in;
+        w.dE = r.dE;
+        w.nodes = r.nodes;
+        if (!isfinite(r.dE) || !isfinite(ck)) w.status |= EPSCU_STATUS_NONFINITE;
+        if (r.nodes != w.v) w.status |= EPSCU_STATUS_NOTFOUND;
+        b.levels[slot] = w;
+    }
+}
+
+__global__ void __launch_bounds__(kLevelThreads) write64_kernel(DevBatch b) {
+    const int total = b.hdr->total_levels;
+    if (!b.psi || b.hdr->error) return;
+    for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < total; slot += gridDim.x * blockDim.x) {
+        const LevelWork w = b.levels[slot];
+        const PotMeta m = b.meta[w.p];
+        double* out = b.psi + m.psi_off + (int64_t)(w.v - b.min_level) * m.N;
+        for (int i = 0; i < m.i0; ++i) out[i] = 0.0;
+        for (int i = m.i1 + 1; i < m.N; ++i) out[i] = 0.0;
+        if (w.status & (EPSCU_STATUS_NOTFOUND | EPSCU_STATUS_CANCELLED | EPSCU_STATUS_NONFINITE)) {
+            for (int i = m.i0; i <= m.i1; ++i) out[i] = 0.0;
+            continue;
+        }
+        const double* W = b.W64 + m.off;
+        const double aE = __dmul_rn(m.a, w.E);
+        Side64 st;
+        side64<true, true>(W, aE, m.i0, w.k, +1, st, out, w.norm_k_out, w.ex_out);
+        side64<true, true>(W, aE, m.i1, w.k, -1, st, out, w.norm_k_in, w.ex_in);
+        out[w.k] = w.ck;
+    }
+}
+
+__global__ void gather_kernel(DevBatch b, int32_t* n_total, int32_t* n_out, double* energy, int32_t* nodes,
+                              int32_t* status, double* err_est, int apply_dE) {
+    const int p = blockIdx.x;
+    const PotMeta m = b.meta[p];
+    if (threadIdx.x == 0) {
+        n_total[p] = m.n_total;
+        n_out[p] = m.n_out;
+    }
+    for (int s = threadIdx.x; s < b.level_capacity; s += blockDim.x) {
+        const int64_t o = (int64_t)p * b.level_capacity + s;
+        if (s < m.n_out) {
+            const LevelWork w = b.levels[m.level_base + s];
+            energy[o] = (apply_dE && fabs(w.dE) <= 1e-9) ? w.E + w.dE : w.E;
+            nodes[o] = w.nodes;
+            status[o] = w.status | (m.status & EPSCU_STATUS_UNDER);
+            if (err_est) err_est[o] = fabs(w.dE);
+        } else {
+            energy[o] = NAN;
+            nodes[o] = -1;
+            status[o] = EPSCU_STATUS_NOTFOUND | (m.status & EPSCU_STATUS_BAD);
+            if (err_est) err_est[o] = NAN;
+        }
+    }
+}
+
+int persistent_grid(int sm_count, int per_sm) { return sm_count * per_sm; }
+
+}  // namespace
+
+void launch_bisect64(const DevBatch& b, int sm_count, cudaStream_t s) {
+    bisect64_kernel<<<persistent_grid(sm_count, 8), kLevelThreads, 0, s>>>(b);
+}
+void launch_refine32(const DevBatch& b, int sm_count, cudaStream_t s) {
+    refine32_kernel<<<persistent_grid(sm_count, 8), kLevelThreads, 0, s>>>(b);
+}
+void launch_newton64(const DevBatch& b, int sm_count, cudaStream_t s) {
+    newton64_kernel<<<persistent_grid(sm_count, 8), kLevelThreads, 0, s>>>(b);
+}
+void launch_norm64(const DevBatch& b, int use_k, int sm_count, cudaStream_t s) {
+    norm64_kernel<<<persistent_grid(sm_count, 8), kLevelThreads, 0, s>>>(b, use_k);
+}
+void launch_write64(const DevBatch& b, int sm_count, cudaStream_t s) {
+    write64_kernel<<<persistent_grid(sm_count, 8), kLevelThreads, 0, s>>>(b);
+}
+void launch_gather(const DevBatch& b, int32_t* n_total, int32_t* n_out, double* energy, int32_t* nodes,
+                   int32_t* status, double* err_est, int apply_dE, cudaStream_t s) {
+    gather_kernel<<<b.n, 128, 0, s>>>(b, n_total, n_out, energy, nodes, status, err_est, apply_dE);
+}
+
+}  // namespace epscu

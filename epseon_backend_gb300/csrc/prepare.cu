@@ -1,0 +1,345 @@
+// prepare.cu -- per-potential set-up of the discrete problem, level-slot
+// bookkeeping and device-side tabulation of parametric potentials.
+//
+// The set-up mirrors the oracle's eo_prepare() exactly (same FP64 operations):
+// minimum of V, E-independent Dirichlet cut-offs (a (V_i - E_lo) <= 1/2),
+// scan twist index (argmin V), trial spacing and the bisection step count.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "common.cuh"
+#include "launch.h"
+
+namespace epscu {
+
+namespace {
+
+constexpr int kPrepThreads = 256;
+
+template <typename T, typename Op>
+__device__ T block_reduce(T v, Op op, T* sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    const int nw = blockDim.x >> 5;
+    v = threadIdx.x < nw ? sh[threadIdx.x] : sh[0];
+    if (warp == 0)
+        for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (threadIdx.x == 0) sh[0] = v;
+    __syncthreads();
+    v = sh[0];
+    __syncthreads();
+    return v;
+}
+
+struct MinOp {
+    __device__ double operator()(double a, double b) const { return fmin(a, b); }
+};
+struct MinI {
+    __device__ int operator()(int a, int b) const { return min(a, b); }
+};
+struct MaxI {
+    __device__ int operator()(int a, int b) const { return max(a, b); }
+};
+struct OrI {
+    __device__ int operator()(int a, int b) const { return a | b; }
+};
+
+__global__ void __launch_bounds__(kPrepThreads) prepare_kernel(DevBatch b) {
+    __shared__ double shd[32];
+    __shared__ int shi[32];
+    const int p = blockIdx.x;
+    PotMeta m = b.meta[p];
+    const double* V = b.V64 + m.off;
+    const int N = m.N;
+    const int tid = threadIdx.x, nt = blockDim.x;
+
+    double vmin = INFINITY;
+    int bad = 0;
+    for (int i = tid; i < N; i += nt) {
+        const double v = V[i];
+        if (!isfinite(v)) bad = 1;
+        vmin = fmin(vmin, v);
+    }
+    vmin = block_reduce(vmin, MinOp(), shd);
+    bad = block_reduce(bad, OrI(), shi);
+
+    const double h = __ddiv_rn(__dsub_rn(m.r_max, m.r_min), (double)(N - 1));
+    const double a = __ddiv_rn(__dmul_rn(__dmul_rn(m.mu, h), h), 6.0);
+    int first = N, last = -1;
+    for (int i = tid; i < N; i += nt) {
+        if (__dmul_rn(a, __dsub_rn(V[i], vmin)) <= 0.5) {
+            first = min(first, i);
+            last = max(last, i);
+        }
+    }
+    first = block_reduce(first, MinI(), shi);
+    last = block_reduce(last, MaxI(), shi);
+    const int i0 = first < 1 ? 1 : first;
+    const int i1 = last > N - 2 ? N - 2 : last;
+
+    // argmin on [i0, i1], first occurrence
+    double bv = INFINITY;
+    int bi = N;
+    for (int i = i0 + tid; i <= i1; i += nt) {
+        const double v = V[i];
+        if (v < bv) {
+            bv = v;
+            bi = i;
+        }
+    }
+    const double gmin = block_reduce(bv, MinOp(), shd);
+    int cand = (bv == gmin) ? bi : N;
+    const int k_scan = block_reduce(cand, MinI(), shi);
+
+    // W = a V in FP64 and as an unevaluated (hi, lo) float pair; zero padding
+    double* W = b.W64 + m.off;
+    float2* Wf = b.Wf2 ? b.Wf2 + m.offf : nullptr;
+    for (int i = tid; i < N; i += nt) {
+        const double w = __dmul_rn(a, V[i]);
+        W[i] = w;
+        if (Wf) {
+            const float hi = __double2float_rn(w);
+            const float lo = __double2float_rn(__dsub_rn(w, (double)hi));
+            Wf[i] = make_float2(hi, lo);
+        }
+    }
+
+    // suffix minima of V on [i0, i1] (chunked block scan, right to left)
+    __shared__ double chunk_min[kPrepThreads];
+    const int n_in = i1 - i0 + 1;
+    const int per = n_in > 0 ? (n_in + nt - 1) / nt : 0;
+    const int c0 = i0 + tid * per;
+    const int c1 = min(c0 + per, i1 + 1);
+    double cm = INFINITY;
+    for (int i = c0; i < c1; ++i) cm = fmin(cm, V[i]);
+    chunk_min[tid] = cm;
+    __syncthreads();
+    if (tid == 0) {
+        double run = INFINITY;
+        for (int t = nt - 1; t >= 0; --t) {
+            const double x = chunk_min[t];
+            chunk_min[t] = run;  // minimum of all chunks to the right of t
+            run = fmin(run, x);
+        }
+    }
+    __syncthreads();
+    double* M = b.Msuf + m.off;
+    double run = chunk_min[tid];
+    for (int i = c1 - 1; i >= c0; --i) {
+        run = fmin(run, V[i]);
+        M[i] = run;
+    }
+
+    if (tid == 0) {
+        int status = 0;
+        if (bad) status |= EPSCU_STATUS_BAD | EPSCU_STATUS_NONFINITE;
+        if (i1 - i0 < 2) status |= EPSCU_STATUS_BAD;
+        if (!(m.e_cap > vmin)) status |= EPSCU_STATUS_BAD;
+        m.h = h;
+        m.a = a;
+        m.e_lo = vmin;
+        m.i0 = i0;
+        m.i1 = i1;
+        m.k_scan = k_scan < N ? k_scan : i0;
+        m.delta = __ddiv_rn(__dsub_rn(m.e_cap, vmin), (double)m.n_trial);
+        const double tol = b.tol > 0.0 ? b.tol : 1e-12;
+        int K = 0;
+        for (double w = m.delta; w > tol && K < 200; w = __dmul_rn(w, 0.5)) ++K;
+        m.n_bisect = K;
+        const double kmax = sqrt(2.0 * m.mu * (m.e_cap - vmin));
+        if (kmax * h > 1.0) status |= EPSCU_STATUS_UNDER;
+        m.status = status;
+        m.n_total = 0;
+        m.n_out = 0;
+        b.meta[p] = m;
+    }
+}
+
+// Level counts per potential, exclusive prefix sums (level slots and psi
+// offsets) and the total level count.  One CTA.
+__global__ void __launch_bounds__(1024) level_setup_kernel(DevBatch b) {
+    __shared__ int32_t s_lv[1024];
+    __shared__ long long s_ps[1024];
+    __shared__ int32_t carry_lv;
+    __shared__ long long carry_ps;
+    if (threadIdx.x == 0) {
+        carry_lv = 0;
+        carry_ps = 0;
+    }
+    __syncthreads();
+    for (int base = 0; base < b.n; base += blockDim.x) {
+        const int p = base + threadIdx.x;
+        int32_t n_out = 0;
+        long long ps = 0;
+        if (p < b.n) {
+            PotMeta& m = b.meta[p];
+            int32_t n_total = 0;
+            if (!(m.status & EPSCU_STATUS_BAD)) n_total = b.counts[(int64_t)p * b.n_trial + b.n_trial - 1];
+            int32_t last = b.max_level < 0 ? n_total - 1 : min(b.max_level, n_total - 1);
+            n_out = last - b.min_level + 1;
+            n_out = max(0, min(n_out, b.level_capacity));
+            m.n_total = n_total;
+            m.n_out = n_out;
+            ps = (long long)n_out * m.N;
+        }
+        s_lv[threadIdx.x] = n_out;
+        s_ps[threadIdx.x] = ps;
+        __syncthreads();
+        // inclusive Hillis-Steele scan
+        for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+            int32_t x = threadIdx.x >= o ? s_lv[threadIdx.x - o] : 0;
+            long long y = threadIdx.x >= o ? s_ps[threadIdx.x - o] : 0;
+            __syncthreads();
+            s_lv[threadIdx.x] += x;
+            s_ps[threadIdx.x] += y;
+            __syncthreads();
+        }
+        if (p < b.n) {
+            b.meta[p].level_base = carry_lv + s_lv[threadIdx.x] - n_out;
+            b.meta[p].psi_off = carry_ps + s_ps[threadIdx.x] - ps;
+        }
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) {
+            carry_lv += s_lv[threadIdx.x];
+            carry_ps += s_ps[threadIdx.x];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        b.hdr->total_levels = carry_lv;
+        b.hdr->queue_refine = 0;
+        b.hdr->queue_polish = 0;
+        if (b.psi && carry_ps > b.psi_capacity) atomicCAS(&b.hdr->error, 0, 5);
+    }
+}
+
+// Bracket of every level slot from the scan counts: first trial j with
+// count_j > v; bracket [E_{j-1}, E_j] (E_{-1} = E_lo).
+__global__ void bracket_kernel(DevBatch b) {
+    const int p = blockIdx.x;
+    const PotMeta m = b.meta[p];
+    const int32_t* c = b.counts + (int64_t)p * b.n_trial;
+    for (int s = threadIdx.x; s < m.n_out; s += blockDim.x) {
+        const int v = b.min_level + s;
+        int lo = 0, hi = m.n_trial;
+        while (lo < hi) {
+            const int mid = lo + (hi - lo) / 2;
+            if (c[mid] > v) hi = mid;
+            else lo = mid + 1;
+        }
+        LevelWork w;
+        w.p = p;
+        w.v = v;
+        w.status = m.status & EPSCU_STATUS_UNDER;
+        w.nodes = -1;
+        w.iters = 0;
+        w.k = m.k_scan;
+        w.dE = 0.0;
+        w.norm_k_out = w.norm_k_in = 0.0;
+        w.ex_out = w.ex_in = 0;
+        if (lo >= m.n_trial) {
+            w.status |= EPSCU_STATUS_NOTFOUND;
+            w.lo = w.hi = w.E = m.e_cap;
+        } else {
+            w.lo = lo == 0 ? m.e_lo : trial_energy(m, lo - 1);
+            w.hi = trial_energy(m, lo);
+            w.E = __dmul_rn(0.5, __dadd_rn(w.lo, w.hi));
+        }
+        b.levels[m.level_base + s] = w;
+    }
+}
+
+// ------------------------------------------------------------- tabulation (K0)
+
+__device__ double morse_v(double r, double De, double a, double re) {
+    const double x = 1.0 - exp(-a * (r - re));
+    return De * x * x;
+}
+
+__global__ void tabulate_kernel(int32_t n, const int32_t* kind, const double* params, const int64_t* offsets,
+                                const int32_t* Ns, const double* r_min, const double* r_max, int32_t n_knots,
+                                double* scratch, double* V) {
+    const int p = blockIdx.x;
+    const int N = Ns[p];
+    const double r0 = r_min[p], r1 = r_max[p];
+    const double h = (r1 - r0) / (double)(N - 1);
+    const double* P = params + (int64_t)p * 12;
+    double* out = V + offsets[p];
+    const int k = kind[p];
+    if (k == EPSCU_KIND_SPLINE) {
+        // knot values (Morse + Gaussian bumps), natural spline second derivatives
+        double* y = scratch + (int64_t)p * 3 * n_knots;
+        double* M = y + n_knots;
+        double* cp = M + n_knots;
+        const double hk = (r1 - r0) / (double)(n_knots - 1);
+        for (int j = threadIdx.x; j < n_knots; j += blockDim.x) {
+            const double r = r0 + j * hk;
+            double v = morse_v(r, P[0], P[1], P[2]);
+            for (int q = 0; q < 3; ++q) {
+                const double amp = P[3 + 3 * q], w = P[4 + 3 * q], c = P[5 + 3 * q];
+                if (amp != 0.0) v += amp * exp(-((r - c) * (r - c)) / (2.0 * w * w));
+            }
+            y[j] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            // Thomas algorithm for M_{k-1} + 4 M_k + M_{k+1} = 6 (y_{k+1} - 2 y_k + y_{k-1}) / hk^2
+            const int nn = n_knots - 2;
+            const double s6 = 6.0 / (hk * hk);
+            M[0] = 0.0;
+            M[n_knots - 1] = 0.0;
+            // forward sweep: cp in cp[], dp in M[1..]
+            cp[0] = 1.0 / 4.0;
+            M[1] = s6 * (y[2] - 2.0 * y[1] + y[0]) / 4.0;
+            for (int i = 1; i < nn; ++i) {
+                const double den = 4.0 - cp[i - 1];
+                cp[i] = 1.0 / den;
+                const double rhs = s6 * (y[i + 2] - 2.0 * y[i + 1] + y[i]);
+                M[i + 1] = (rhs - M[i]) / den;
+            }
+            for (int i = nn - 2; i >= 0; --i) M[i + 1] = M[i + 1] - cp[i] * M[i + 2];
+        }
+        __syncthreads();
+        const double h2 = hk * hk / 6.0;
+        for (int i = threadIdx.x; i < N; i += blockDim.x) {
+            const double r = r0 + i * h;
+            const double t = (r - r0) / hk;
+            int j = (int)floor(t);
+            j = max(0, min(j, n_knots - 2));
+            const double u = t - j, w = 1.0 - u;
+            out[i] = w * y[j] + u * y[j + 1] + h2 * ((w * w * w - w) * M[j] + (u * u * u - u) * M[j + 1]);
+        }
+    } else if (k == EPSCU_KIND_LJ) {
+        const double eps = P[0], sigma = P[1];
+        for (int i = threadIdx.x; i < N; i += blockDim.x) {
+            const double r = r0 + i * h;
+            const double s = sigma / r;
+            const double s2 = s * s;
+            const double s6 = s2 * s2 * s2;
+            out[i] = 4.0 * eps * (s6 * s6 - s6) + eps;
+        }
+    } else {
+        for (int i = threadIdx.x; i < N; i += blockDim.x) out[i] = morse_v(r0 + i * h, P[0], P[1], P[2]);
+    }
+}
+
+}  // namespace
+
+void launch_prepare(const DevBatch& b, cudaStream_t s) {
+    prepare_kernel<<<b.n, kPrepThreads, 0, s>>>(b);
+}
+
+void launch_level_setup(const DevBatch& b, cudaStream_t s) {
+    level_setup_kernel<<<1, 1024, 0, s>>>(b);
+    bracket_kernel<<<b.n, 128, 0, s>>>(b);
+}
+
+void launch_tabulate(int32_t n, const int32_t* kind, const double* params, const int64_t* offsets, const int32_t* N,
+                     const double* r_min, const double* r_max, int32_t n_knots, double* knot_scratch, double* V,
+                     cudaStream_t s) {
+    tabulate_kernel<<<n, 256, 0, s>>>(n, kind, params, offsets, N, r_min, r_max, n_knots, knot_scratch, V);
+}
+
+}  // namespace epscu

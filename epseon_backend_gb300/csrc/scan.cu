@@ -1,0 +1,326 @@
+// scan.cu -- trial-energy scan: Sturm counts at the n_trial trial energies
+// of every potential.
+//
+//  scan64 : the plain method.  One thread per trial energy, FP64 projective
+//           Numerov outward to the twist index and inward to it, arithmetic
+//           identical to the oracle's eo_count (bit-exact counts).
+//  scan32 : the fast method.  Persistent CTAs pull (potential, energy block)
+//           work items from a device queue, ordered longest grid first.  Each
+//           potential's W = a V is staged into shared memory tile by tile with
+//           1-D bulk TMA copies (cp.async.bulk + mbarrier, STAGES deep) and
+//           read as warp-wide broadcasts.  Each thread carries one trial
+//           energy through the FP32 difference-form recurrence
+//             D' = D + T (D - 12 A),  A' = A + (T A + D')
+//           (A ~ u_i, D ~ u_i - u_{i-1}; Blatt 1967) with T = aE - W held as an
+//           unevaluated pair of floats, so the count is reliable to
+//           |E - E_v| ~ 1e-9 Hartree.  The twist pivot is evaluated in FP64 in
+//           the cancellation-free form -12 T_k A C + f_k (D_o C + D_i A).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "launch.h"
+
+namespace epscu {
+
+namespace {
+
+constexpr int kScan64Threads = 128;
+
+__global__ void __launch_bounds__(kScan64Threads) scan64_kernel(DevBatch b, int ipp) {
+    const int item = blockIdx.x;
+    const int p = b.order[item / ipp];
+    const int blk = item % ipp;
+    const PotMeta m = b.meta[p];
+    const int j = blk * kScan64Threads + threadIdx.x;
+    if (j >= b.n_trial) return;
+    int32_t c = 0;
+    if (!(m.status & EPSCU_STATUS_BAD)) c = count64(m, b.W64 + m.off, trial_energy(m, j), m.k_scan);
+    b.counts[(int64_t)p * b.n_trial + j] = c;
+}
+
+// ------------------------------------------------------------------ TMA plumbing
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait on a phase of an mbarrier; false when the limit ran out.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+    for (int it = 0; it < (1 << 22); ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void fence_barrier_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Tile t of the item's sequence: outward tiles ascending over [i0, k-1], then
+// inward tiles descending over [k+1, i1].
+struct TileSeq {
+    int out_first, n_out, in_first, n_in;  // tile indices
+    __device__ int tile(int t) const { return t < n_out ? out_first + t : in_first - (t - n_out); }
+    __device__ int size() const { return n_out + n_in; }
+};
+
+__device__ __forceinline__ TileSeq make_seq(const PotMeta& m, int tile) {
+    TileSeq s;
+    const int k = m.k_scan;
+    if (k > m.i0) {
+        s.out_first = m.i0 / tile;
+        s.n_out = (k - 1) / tile - s.out_first + 1;
+    } else {
+        s.out_first = 0;
+        s.n_out = 0;
+    }
+    if (k < m.i1) {
+        s.in_first = m.i1 / tile;
+        s.n_in = s.in_first - (k + 1) / tile + 1;
+    } else {
+        s.in_first = 0;
+        s.n_in = 0;
+    }
+    return s;
+}
+
+__device__ __forceinline__ void renorm_f(float& A, float& D) {
+    const float m = fmaxf(fabsf(A), fabsf(D));
+    const int e = ((__float_as_int(m) >> 23) & 0xff) - 126;
+    if (m > 0.0f && e > -100 && e < 100) {
+        const float s = __int_as_float((127 - e) << 23);
+        A *= s;
+        D *= s;
+    }
+}
+
+// One FP32 difference-form step at a point with W = (w.x + w.y).
+__device__ __forceinline__ void step32(float aEh, float aEl, float2 w, float& A, float& D, int& nodes) {
+    const float T = (aEh - w.x) + (aEl - w.y);
+    const float X = fmaf(-12.0f, A, D);
+    D = fmaf(T, X, D);
+    const float inc = fmaf(T, A, D);
+    const float An = A + inc;
+    nodes += (__float_as_uint(An) ^ __float_as_uint(A)) >> 31;
+    A = An;
+}
+
+template <int THREADS, int TILE, int STAGES>
+__global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, int n_items) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float2* buf = reinterpret_cast<float2*>(smem_raw);
+    __shared__ __align__(8) uint64_t full[STAGES];
+    __shared__ int s_item;
+    __shared__ int s_abort;
+
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        for (int s = 0; s < STAGES; ++s) mbar_init(&full[s], 1);
+        fence_barrier_init();
+        s_abort = 0;
+    }
+    __syncthreads();
+
+    uint32_t g_tile = 0;   // tiles consumed by this CTA so far (phase bookkeeping)
+    uint32_t g_issue = 0;  // tiles issued by this CTA so far (thread 0)
+    for (;;) {
+        __syncthreads();  // everyone has read the previous s_item
+        if (tid == 0) {
+            int it = atomicAdd(&b.hdr->queue_scan, 1);
+            if (b.cancel && *b.cancel) it = n_items;
+            s_item = it;
+        }
+        __syncthreads();
+        const int item = s_item;
+        if (item >= n_items || s_abort) break;
+        const int p = b.order[item / ipp];
+        const int j = (item % ipp) * THREADS + tid;
+        const PotMeta m = b.meta[p];
+        if (m.status & EPSCU_STATUS_BAD) {
+            if (j < b.n_trial) b.counts[(int64_t)p * b.n_trial + j] = 0;
+            continue;  // uniform across the CTA
+        }
+        const TileSeq seq = make_seq(m, TILE);
+        const int L = seq.size();
+        const float2* src = b.Wf2 + m.offf;
+
+        // prologue: up to STAGES tiles in flight
+        if (tid == 0) {
+            fence_proxy_async();
+            for (int t = 0; t < STAGES && t < L; ++t) {
+                const int st = (g_tile + t) % STAGES;
+                mbar_expect_tx(&full[st], TILE * sizeof(float2));
+                bulk_load(buf + st * TILE, src + (int64_t)seq.tile(t) * TILE, TILE * sizeof(float2), &full[st]);
+                ++g_issue;
+            }
+        }
+
+        const double E = trial_energy(m, min(j, b.n_trial - 1));
+        const double aE = __dmul_rn(m.a, E);
+        const float aEh = __double2float_rn(aE);
+        const float aEl = __double2float_rn(aE - (double)aEh);
+        const int k = m.k_scan;
+        float A = 1.0f, D = 1.0f;  // u_{i0} = 1, u_{i0-1} = 0
+        float Ao = 1.0f, Do = 1.0f;
+        int nodes = 0;
+        int steps = 0;
+        bool inward = false;
+
+        for (int t = 0; t < L; ++t) {
+            const int st = (g_tile + t) % STAGES;
+            const uint32_t par = ((g_tile + t) / STAGES) & 1u;
+            if (!mbar_wait_bounded(&full[st], par)) {
+                atomicExch(&s_abort, 1);
+                atomicCAS(&b.hdr->error, 0, EPSCU_ERR_TIMEOUT);
+            }
+            const float2* tb = buf + st * TILE;
+            const int T0 = seq.tile(t) * TILE;
+            if (t < seq.n_out) {
+                const int a0 = max(m.i0, T0), a1 = min(k - 1, T0 + TILE - 1);
+                for (int i = a0; i <= a1; ++i) {
+                    step32(aEh, aEl, tb[i - T0], A, D, nodes);
+                    if ((++steps & 15) == 0) renorm_f(A, D);
+                }
+            } else {
+                if (!inward) {
+                    inward = true;
+                    Ao = A;
+                    Do = D;
+                    A = 1.0f;  // v_{i1} = 1, v_{i1+1} = 0
+                    D = 1.0f;
+                    steps = 0;
+                }
+                const int a0 = min(m.i1, T0 + TILE - 1), a1 = max(k + 1, T0);
+                for (int i = a0; i >= a1; --i) {
+                    step32(aEh, aEl, tb[i - T0], A, D, nodes);
+                    if ((++steps & 15) == 0) renorm_f(A, D);
+                }
+            }
+            __syncthreads();  // every thread is done with stage st
+            if (s_abort) {
+                g_tile += t;  // tiles t.. were issued but not consumed
+                break;
+            }
+            if (tid == 0 && t + STAGES < L) {
+                fence_proxy_async();
+                mbar_expect_tx(&full[st], TILE * sizeof(float2));
+                bulk_load(buf + st * TILE, src + (int64_t)seq.tile(t + STAGES) * TILE, TILE * sizeof(float2),
+                          &full[st]);
+                ++g_issue;
+            }
+        }
+        if (s_abort) break;
+        g_tile += L;
+        if (!inward) {  // no inward tiles: k == i1
+            Ao = A;
+            Do = D;
+            A = 1.0f;
+            D = 1.0f;
+        }
+        // twist pivot sign in FP64: -12 T_k u_k v_k + f_k (D_o v_k + D_i u_k)
+        const double Tk = aE - b.W64[m.off + k];
+        const double fk = 1.0 + Tk;
+        const double uA = (double)Ao, vC = (double)A;
+        const double AC = uA * vC;
+        const double num = -12.0 * Tk * AC + fk * ((double)Do * vC + (double)D * uA);
+        nodes += (num < 0.0) != (AC < 0.0);
+        if (j < b.n_trial) b.counts[(int64_t)p * b.n_trial + j] = nodes;
+    }
+    __syncthreads();
+    if (s_abort && tid == 0) {
+        // drain: wait (bounded) for the copies issued but never consumed
+        for (uint32_t q = g_tile; q < g_issue; ++q) (void)mbar_wait_bounded(&full[q % STAGES], (q / STAGES) & 1u);
+    }
+}
+
+template <int THREADS, int TILE, int STAGES>
+void launch_scan32_t(const DevBatch& b, int ctas_per_sm, int sm_count, cudaStream_t s) {
+    const int ipp = (b.n_trial + THREADS - 1) / THREADS;
+    const int n_items = ipp * b.n;
+    const size_t smem = (size_t)TILE * STAGES * sizeof(float2);
+    auto kern = scan32_kernel<THREADS, TILE, STAGES>;
+    if (ctas_per_sm <= 0) {
+        int occ = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, THREADS, smem);
+        ctas_per_sm = occ > 0 ? occ : 1;
+    }
+    int grid = sm_count * ctas_per_sm;
+    if (grid > n_items) grid = n_items;
+    if (grid < 1) grid = 1;
+    kern<<<grid, THREADS, smem, s>>>(b, ipp, n_items);
+}
+
+template <int THREADS, int TILE, int STAGES>
+void set_attr_t() {
+    cudaFuncSetAttribute(scan32_kernel<THREADS, TILE, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(TILE * STAGES * sizeof(float2)));
+}
+
+}  // namespace
+
+void scan32_set_attributes() {
+    set_attr_t<128, 1024, 4>();
+    set_attr_t<128, 2048, 3>();
+    set_attr_t<256, 1024, 4>();
+    set_attr_t<256, 2048, 3>();
+    set_attr_t<256, 4096, 2>();
+    set_attr_t<512, 1024, 4>();
+    set_attr_t<512, 2048, 3>();
+}
+
+void launch_scan64(const DevBatch& b, cudaStream_t s) {
+    const int ipp = (b.n_trial + kScan64Threads - 1) / kScan64Threads;
+    scan64_kernel<<<ipp * b.n, kScan64Threads, 0, s>>>(b, ipp);
+}
+
+int scan32_max_tile() { return 4096; }
+
+void launch_scan32(const DevBatch& b, const ScanShape& sh, int sm_count, cudaStream_t s) {
+#define EPSCU_SCAN32_CASE(TH, TI, ST)                                              \
+    if (sh.threads == TH && sh.tile == TI && sh.stages == ST) {                    \
+        launch_scan32_t<TH, TI, ST>(b, sh.ctas_per_sm, sm_count, s);               \
+        return;                                                                    \
+    }
+    EPSCU_SCAN32_CASE(128, 1024, 4)
+    EPSCU_SCAN32_CASE(128, 2048, 3)
+    EPSCU_SCAN32_CASE(256, 1024, 4)
+    EPSCU_SCAN32_CASE(256, 2048, 3)
+    EPSCU_SCAN32_CASE(256, 4096, 2)
+    EPSCU_SCAN32_CASE(512, 1024, 4)
+    EPSCU_SCAN32_CASE(512, 2048, 3)
+#undef EPSCU_SCAN32_CASE
+    launch_scan32_t<256, 2048, 3>(b, sh.ctas_per_sm, sm_count, s);
+}
+
+}  // namespace epscu

@@ -1,0 +1,132 @@
+"""Parity of the CUDA solver (through the C ABI) with the FP64 oracle.
+
+Tolerances (spec bar): node counts bit-exact; energies within 1e-10
+Hartree for the plain FP64 method (bit-exact here, same arithmetic as the
+oracle) and 1e-9 for the FP32-compensated method; normalised wavefunctions
+within 1e-8 in L2 (sum (psi - psi_ref)^2 h).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from epseon_backend_gb300 import capi, synth
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+E_TOL_PLAIN = 1e-10
+E_TOL_FAST = 1e-9
+PSI_TOL = 1e-8
+
+
+def _oracle(b, want_psi=False, idx=None):
+    idx = range(len(b)) if idx is None else idx
+    Vs = [b.V(i) for i in idx]
+    sel = np.array(list(idx))
+    return O.solve_batch(Vs, b.r_min[sel], b.r_max[sel], b.mu[sel], b.e_cap[sel], b.n_trial, want_psi=want_psi)
+
+
+def _gpu(ctx, b, method, want_psi=False, idx=None, cap=512):
+    idx = list(range(len(b))) if idx is None else list(idx)
+    Vs = [b.V(i) for i in idx]
+    sel = np.array(idx)
+    return ctx.solve(Vs, b.r_min[sel], b.r_max[sel], b.mu[sel], b.e_cap[sel], b.n_trial, method=method,
+                     want_psi=want_psi, level_capacity=cap)
+
+
+def _psi_l2(a, b, h):
+    return float(np.sqrt(np.sum((a - b) ** 2) * h))
+
+
+@pytest.mark.parametrize("method", [capi.METHOD_PLAIN_FP64, capi.METHOD_FAST_FP32C])
+def test_morse_single(ctx, method):
+    b = synth.morse_single()
+    ref = _oracle(b, want_psi=True)[0]
+    sol = _gpu(ctx, b, method, want_psi=True, cap=32)
+    assert sol.n_total[0] == ref.n_total == 14
+    n = sol.n_out[0]
+    assert n == 14
+    assert np.array_equal(sol.nodes[0, :n], np.arange(n))
+    assert np.all(sol.status[0, :n] == 0)
+    if method == capi.METHOD_PLAIN_FP64:
+        # same arithmetic as the oracle: identical bits
+        assert np.array_equal(sol.energy[0, :n], ref.energy)
+    else:
+        assert np.max(np.abs(sol.energy[0, :n] - ref.energy_polished)) < E_TOL_FAST
+    h = ref.grid.h
+    psi = sol.wavefunctions(0)
+    for v in range(n):
+        assert _psi_l2(psi[v], ref.psi[v], h) < PSI_TOL
+        assert abs(np.sum(psi[v] ** 2) * h - 1.0) < 1e-12
+
+
+@pytest.mark.parametrize("method", [capi.METHOD_PLAIN_FP64, capi.METHOD_FAST_FP32C])
+def test_morse_batch_subset(ctx, method):
+    b = synth.morse_batch()
+    idx = [0, 5, 17, 42]
+    refs = _oracle(b, idx=idx)
+    sol = _gpu(ctx, b, method, idx=idx)
+    for q, ref in enumerate(refs):
+        n = sol.n_out[q]
+        assert sol.n_total[q] == ref.n_total
+        assert n == ref.energy.size
+        assert np.array_equal(sol.nodes[q, :n], np.arange(n))
+        if method == capi.METHOD_PLAIN_FP64:
+            assert np.array_equal(sol.energy[q, :n], ref.energy)
+        else:
+            assert np.max(np.abs(sol.energy[q, :n] - ref.energy_polished)) < E_TOL_FAST
+
+
+@pytest.mark.parametrize("method", [capi.METHOD_PLAIN_FP64, capi.METHOD_FAST_FP32C])
+def test_mixed_subset(ctx, method):
+    b = synth.mixed_batch()
+    # one of each kind, short grids so the oracle finishes in seconds
+    idx = []
+    for kind in (synth.KIND_MORSE, synth.KIND_LJ, synth.KIND_SPLINE):
+        cand = np.where((b.kind == kind) & (b.N < 6000))[0]
+        idx += list(cand[:2])
+    bb = b.subset(idx)
+    bb.n_trial = 2048
+    refs = _oracle(bb)
+    sol = _gpu(ctx, bb, method)
+    for q, ref in enumerate(refs):
+        n = sol.n_out[q]
+        assert sol.n_total[q] == ref.n_total
+        assert np.array_equal(sol.nodes[q, :n], np.arange(n))
+        if method == capi.METHOD_PLAIN_FP64:
+            assert np.array_equal(sol.energy[q, :n], ref.energy)
+        else:
+            assert np.max(np.abs(sol.energy[q, :n] - ref.energy_polished)) < E_TOL_FAST
+
+
+def test_tabulate_matches_host(ctx):
+    b = synth.mixed_batch(B=12, n_min=2048, n_max=8192)
+    Vd = ctx.tabulate(b.kind, capi.batch_params(b), b.N, b.r_min, b.r_max)
+    for i in range(len(b)):
+        Vh = b.V(i)
+        scale = np.maximum(1.0, np.abs(Vh))
+        assert np.max(np.abs(Vd[i] - Vh) / scale) < 1e-11
+
+
+def test_adjoint_matches_finite_differences(ctx):
+    b = synth.morse_single(N=2048, n_trial=512)
+    V = b.V(0).copy()
+    sol = ctx.solve([V], b.r_min, b.r_max, b.mu, b.e_cap, b.n_trial, method=capi.METHOD_PLAIN_FP64,
+                    want_psi=True, level_capacity=16)
+    n = sol.n_out[0]
+    rng = np.random.default_rng(0)
+    w = rng.uniform(0.5, 1.0, n)
+    gE = np.zeros((1, 16))
+    gE[0, :n] = w
+    gV = ctx.adjoint(gE, V.size)
+    g = O.grid(V, b.r_min[0], b.r_max[0], b.mu[0], b.e_cap[0], b.n_trial)
+    for i in [g.i0 + 200, 300, 500, 700]:
+        hfd = 1e-6
+        Vp, Vm = V.copy(), V.copy()
+        Vp[i] += hfd
+        Vm[i] -= hfd
+        rp = O.solve_batch([Vp], b.r_min, b.r_max, b.mu, b.e_cap, b.n_trial)[0]
+        rm = O.solve_batch([Vm], b.r_min, b.r_max, b.mu, b.e_cap, b.n_trial)[0]
+        fd = np.sum(w * (rp.energy_polished - rm.energy_polished)) / (2 * hfd)
+        assert abs(gV[i] - fd) <= 1e-6 * max(abs(fd), 1e-3)
