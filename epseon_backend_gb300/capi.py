@@ -364,3 +364,77 @@ def batch_params(b) -> np.ndarray:
             P[i, 0:3] = b.morse[i]
             P[i, 3:12] = b.bumps[i].reshape(-1)
     return P
+
+
+class DeviceBatch:
+    """A batch resident in device memory (torch tensors) with persistent output
+    buffers, solved through the C ABI with EPSCU_MEM_DEVICE; repeated solves of
+    the same DeviceBatch replay the context's captured CUDA graph."""
+
+    def __init__(self, ctx: Context, Vs, r_min, r_max, mu, e_cap, n_trial: int, level_capacity: int,
+                 min_level: int = 0, max_level: int = -1, want_psi: bool = True, psi_capacity: int | None = None,
+                 device: str = "cuda"):
+        import torch
+
+        self.ctx = ctx
+        V, offsets, N = concat(Vs)
+        n = len(Vs)
+
+        def arr(x):
+            a = np.asarray(x, np.float64)
+            return np.ascontiguousarray(np.broadcast_to(a, (n,)) if a.ndim == 0 else a)
+
+        self.n = n
+        self.N = N
+        self.offsets = offsets
+        self.r_min, self.r_max, self.mu, self.e_cap = arr(r_min), arr(r_max), arr(mu), arr(e_cap)
+        self.n_trial = int(n_trial)
+        self.cap = int(level_capacity)
+        self.min_level, self.max_level = int(min_level), int(max_level)
+        self.total_points = int(V.size)
+        self.V = torch.from_numpy(V).to(device)
+        self.n_total = torch.zeros(n, dtype=torch.int32, device=device)
+        self.n_out = torch.zeros(n, dtype=torch.int32, device=device)
+        self.energy = torch.zeros((n, self.cap), dtype=torch.float64, device=device)
+        self.nodes = torch.zeros((n, self.cap), dtype=torch.int32, device=device)
+        self.status = torch.zeros((n, self.cap), dtype=torch.int32, device=device)
+        self.err = torch.zeros((n, self.cap), dtype=torch.float64, device=device)
+        self.want_psi = want_psi
+        if want_psi:
+            if psi_capacity is None:
+                psi_capacity = int(N.astype(np.int64).sum()) * self.cap
+            self.psi = torch.zeros(int(psi_capacity), dtype=torch.float64, device=device)
+        else:
+            self.psi = None
+        self.psi_offsets = np.zeros(n, np.int64)
+        self.gV = torch.zeros(self.total_points, dtype=torch.float64, device=device)
+        self.psi_required = 0
+
+    def _ptr(self, t, ty):
+        return C.cast(C.c_void_p(t.data_ptr()), ty) if t is not None else None
+
+    def solve(self, method: int = METHOD_FAST_FP32C, tune: bool = False, stage_timing: bool = False, stream=None):
+        import torch
+
+        b = Batch(self.n, self._ptr(self.V, _dp), _l(self.offsets), _i(self.N), _d(self.r_min), _d(self.r_max),
+                  _d(self.mu), _d(self.e_cap), self.n_trial, self.min_level, self.max_level)
+        r = Result(self.cap, self._ptr(self.n_total, _ip), self._ptr(self.n_out, _ip), self._ptr(self.energy, _dp),
+                   self._ptr(self.nodes, _ip), self._ptr(self.status, _ip), self._ptr(self.err, _dp),
+                   self._ptr(self.psi, _dp), int(self.psi.numel()) if self.psi is not None else 0,
+                   _l(self.psi_offsets), 0)
+        flags = MEM_DEVICE | (WANT_PSI if self.want_psi else 0) | (STAGE_TIMING if stage_timing else 0)
+        s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        o = Opts(int(method), flags, 1e-12, C.c_void_p(s), 1 if tune else 0, 0)
+        _check(self.ctx._lib.epscu_solve(self.ctx.handle, C.byref(b), C.byref(r), C.byref(o)))
+        self.psi_required = r.psi_required
+
+    def adjoint(self, gE, recompute: bool = False, stream=None):
+        """dL/dV into self.gV (device) for dL/dE = gE ([n, cap] float64 cuda tensor)."""
+        import torch
+
+        s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        o = Opts(0, MEM_DEVICE, 0.0, C.c_void_p(s), 0, 0)
+        g = gE.contiguous()
+        _check(self.ctx._lib.epscu_adjoint(self.ctx.handle, self._ptr(g, _dp), self._ptr(self.gV, _dp),
+                                           1 if recompute else 0, C.byref(o)))
+        return self.gV

@@ -44,6 +44,7 @@ struct PotMeta {
 // One level slot of the refinement stages.
 struct LevelWork {
     double lo, hi;      // bracket (count(lo) <= v < count(hi))
+    double lo0, hi0;    // the scan bracket
     double E;           // current energy
     double dE;          // last correction (error estimate)
     double norm_k_out;  // write-pass constants: psi scale on the outward side
@@ -63,9 +64,12 @@ struct Header {
     int32_t queue_refine;
     int32_t queue_polish;
     int32_t error;          // first device-side error code (0 = none)
-    int32_t fallbacks;
+    int32_t fallbacks;      // levels that needed the bisection fallback
     int32_t pad[2];
 };
+
+// internal level flag: the Newton stage handed the level to the bisection fallback
+#define EPSCU_STATUS_FALLBACK 0x10000
 
 // ---------------------------------------------------------------- FP64 helpers
 

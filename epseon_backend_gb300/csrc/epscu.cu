@@ -8,8 +8,9 @@
 //
 // Solve pipeline (every stage on the context's stream):
 //   prepare -> scan (FP64 | FP32 TMA persistent) -> level set-up + brackets
-//   plain : bisect64 -> norm64 -> write64
-//   fast  : refine32 -> newton64 -> norm64 -> write64
+//   plain : bisect64 -> norm64 -> write64                      (native FP64)
+//   fast  : refine32 -> newton_df -> norm_df -> write_df       (FP32, then
+//           compensated FP32 with FP64 matching and norm integral)
 //   -> gather into the caller's layout.
 #include <cuda_runtime.h>
 
@@ -44,6 +45,10 @@ epscu_status fail(epscu_status s, const std::string& msg) {
                         std::string(#call) + ": " + cudaGetErrorString(e_));                        \
     } while (0)
 
+// The caller's stream (NULL: the legacy default stream) orders the inputs and
+// receives the outputs; the work itself runs on the context's stream.
+inline cudaStream_t caller_stream(const epscu_opts& o) { return o.stream ? (cudaStream_t)o.stream : cudaStreamLegacy; }
+
 struct DevBuf {
     void* p = nullptr;
     size_t cap = 0;
@@ -63,6 +68,7 @@ struct epscu_ctx {
     volatile int32_t* cancel_host = nullptr;
     int32_t* cancel_dev = nullptr;
     cudaEvent_t ev[kStageEvents] = {};
+    cudaEvent_t ev_in = nullptr, ev_out = nullptr;  // ordering with the caller's stream
     // last solve (kept for the adjoint)
     DevBatch last{};
     bool have_last = false;
@@ -88,6 +94,8 @@ struct epscu_ctx {
         if (cancel_host) cudaFreeHost((void*)cancel_host);
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
+        if (ev_in) cudaEventDestroy(ev_in);
+        if (ev_out) cudaEventDestroy(ev_out);
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -211,6 +219,8 @@ epscu_status epscu_create(int32_t device_ordinal, epscu_ctx** out) {
         e = cudaHostGetDevicePointer((void**)&c->cancel_dev, hc, 0);
     }
     for (int i = 0; i < kStageEvents && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_out, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         delete c;
         return fail(EPSCU_ERR_CUDA, std::string("context set-up: ") + cudaGetErrorString(e));
@@ -281,14 +291,18 @@ void enqueue_pipeline(epscu_ctx* ctx, const DevBatch& b, int method, bool want_p
     if (method == EPSCU_METHOD_PLAIN_FP64) {
         launch_bisect64(b, ctx->sm_count, s);
         rec(3);
+        launch_norm64(b, 0, ctx->sm_count, s);
+        rec(4);
+        if (want_psi) launch_write64(b, ctx->sm_count, s);
     } else {
         launch_refine32(b, ctx->sm_count, s);
         rec(3);
-        launch_newton64(b, ctx->sm_count, s);
+        launch_newton_df(b, ctx->sm_count, s);
+        launch_fallback_df(b, ctx->sm_count, s);
+        launch_norm_df(b, ctx->sm_count, s);
+        rec(4);
+        if (want_psi) launch_write_df(b, ctx->sm_count, s);
     }
-    launch_norm64(b, method == EPSCU_METHOD_FAST_FP32C ? 1 : 0, ctx->sm_count, s);
-    rec(4);
-    if (want_psi) launch_write64(b, ctx->sm_count, s);
     rec(5);
 }
 
@@ -365,7 +379,10 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     std::memcpy(ho, ord.data(), sizeof(int32_t) * n);
 
     // ---- device buffers
-    cudaStream_t s = opts.stream ? (cudaStream_t)opts.stream : ctx->stream;
+    cudaStream_t s = ctx->stream;
+    const cudaStream_t caller = caller_stream(opts);
+    EPSCU_CU(cudaEventRecord(ctx->ev_in, caller));
+    EPSCU_CU(cudaStreamWaitEvent(s, ctx->ev_in, 0));
     const int64_t lv = (int64_t)n * cap;
     DevBatch b{};
     b.n = n;
@@ -375,10 +392,12 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     b.Wf2 = method == EPSCU_METHOD_FAST_FP32C ? (float2*)ctx->get("Wf2", sizeof(float2) * total_padded, &ce) : nullptr;
     b.counts = (int32_t*)ctx->get("counts", sizeof(int32_t) * (size_t)n * batch->n_trial, &ce);
     b.levels = (LevelWork*)ctx->get("levels", sizeof(LevelWork) * lv, &ce);
+    b.fallback_list = (int32_t*)ctx->get("fallback_list", sizeof(int32_t) * lv, &ce);
     b.hdr = (Header*)ctx->get("hdr", sizeof(Header), &ce);
     b.order = (int32_t*)ctx->get("order", sizeof(int32_t) * n, &ce);
     int64_t* d_off = (int64_t*)ctx->get("offsets", sizeof(int64_t) * n, &ce);
-    if (ce != cudaSuccess || !b.meta || !b.W64 || !b.Msuf || !b.counts || !b.levels || !b.hdr || !b.order || !d_off ||
+    if (ce != cudaSuccess || !b.meta || !b.W64 || !b.Msuf || !b.counts || !b.levels || !b.fallback_list || !b.hdr ||
+        !b.order || !d_off ||
         (method == EPSCU_METHOD_FAST_FP32C && !b.Wf2))
         return fail(EPSCU_ERR_NOMEM, std::string("device arena: ") + cudaGetErrorString(ce));
     if (dev) {
@@ -473,7 +492,7 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
                   batch->n_trial, batch->min_level, batch->max_level, (const void*)b.V64, (void*)b.psi,
                   (void*)o_e, (void*)o_nt, (void*)o_no, (void*)o_nd, (void*)o_st, (void*)o_err,
                   (long long)b.psi_capacity, method, cap, shape.threads, shape.tile, shape.stages, opts.tol,
-                  (void*)s);
+                  (void*)s);  // s is the context's own stream
     const std::string gkey = std::string(keybuf) + "|" + std::to_string(total_points);
 
     auto enqueue_all = [&]() -> cudaError_t {
@@ -531,6 +550,8 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     }
     EPSCU_CU(cudaMemcpyAsync(hm, b.meta, sizeof(PotMeta) * n, cudaMemcpyDeviceToHost, s));
     EPSCU_CU(cudaMemcpyAsync(hh, b.hdr, sizeof(Header), cudaMemcpyDeviceToHost, s));
+    EPSCU_CU(cudaEventRecord(ctx->ev_out, s));
+    EPSCU_CU(cudaStreamWaitEvent(caller, ctx->ev_out, 0));
     EPSCU_CU(cudaStreamSynchronize(s));
     EPSCU_CU(cudaGetLastError());
 
@@ -580,7 +601,7 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     st.n_levels = nlev;
     st.fallbacks = hh->fallbacks;
     st.psi_bytes = want_psi ? psi_total * 8 : 0;
-    st.kernel_launches = 7 + (want_psi ? 1 : 0) + (method == EPSCU_METHOD_FAST_FP32C ? 1 : 0);
+    st.kernel_launches = 7 + (want_psi ? 1 : 0) + (method == EPSCU_METHOD_FAST_FP32C ? 2 : 0);
     if (method == EPSCU_METHOD_PLAIN_FP64) {
         st.refine_point_updates = 0;
         int64_t bis = 0;
@@ -617,7 +638,10 @@ extern "C" epscu_status epscu_adjoint(epscu_ctx* ctx, const double* dL_dE, doubl
     cudaSetDevice(ctx->device);
     if (!ctx->have_last) return fail(EPSCU_ERR_INVALID, "no solve to differentiate on this context");
     DevBatch b = ctx->last;
-    cudaStream_t s = opts.stream ? (cudaStream_t)opts.stream : ctx->stream;
+    cudaStream_t s = ctx->stream;
+    const cudaStream_t caller = caller_stream(opts);
+    EPSCU_CU(cudaEventRecord(ctx->ev_in, caller));
+    EPSCU_CU(cudaStreamWaitEvent(s, ctx->ev_in, 0));
     cudaError_t ce = cudaSuccess;
     if (!ctx->last_psi) {
         if (!recompute) return fail(EPSCU_ERR_INVALID, "last solve kept no wavefunctions; pass recompute=1");
@@ -644,6 +668,8 @@ extern "C" epscu_status epscu_adjoint(epscu_ctx* ctx, const double* dL_dE, doubl
     launch_adjoint(b, gE, gV, ctx->last_total_points, ctx->last_offsets_dev, recompute, ctx->sm_count, s);
     EPSCU_CU(cudaGetLastError());
     if (!dev) EPSCU_CU(cudaMemcpyAsync(dL_dV, gV, sizeof(double) * ctx->last_total_points, cudaMemcpyDeviceToHost, s));
+    EPSCU_CU(cudaEventRecord(ctx->ev_out, s));
+    EPSCU_CU(cudaStreamWaitEvent(caller, ctx->ev_out, 0));
     EPSCU_CU(cudaStreamSynchronize(s));
     return EPSCU_OK;
 }
@@ -658,7 +684,10 @@ extern "C" epscu_status epscu_tabulate(epscu_ctx* ctx, int32_t n, const int32_t*
     if (opts_in) opts = *opts_in;
     std::lock_guard<std::mutex> guard(ctx->mu);
     cudaSetDevice(ctx->device);
-    cudaStream_t s = opts.stream ? (cudaStream_t)opts.stream : ctx->stream;
+    cudaStream_t s = ctx->stream;
+    const cudaStream_t caller = caller_stream(opts);
+    EPSCU_CU(cudaEventRecord(ctx->ev_in, caller));
+    EPSCU_CU(cudaStreamWaitEvent(s, ctx->ev_in, 0));
     const bool dev = (opts.flags & EPSCU_MEM_DEVICE) != 0;
     int64_t total = 0;
     // host copies of the per-potential arrays (always host-side per the ABI)
@@ -689,6 +718,8 @@ extern "C" epscu_status epscu_tabulate(epscu_ctx* ctx, int32_t n, const int32_t*
     launch_tabulate(n, d_kind, d_par, d_off, d_N, d_r0, d_r1, n_knots, d_scr, out, s);
     EPSCU_CU(cudaGetLastError());
     if (!dev) EPSCU_CU(cudaMemcpyAsync(V, out, sizeof(double) * total, cudaMemcpyDeviceToHost, s));
+    EPSCU_CU(cudaEventRecord(ctx->ev_out, s));
+    EPSCU_CU(cudaStreamWaitEvent(caller, ctx->ev_out, 0));
     EPSCU_CU(cudaStreamSynchronize(s));
     return EPSCU_OK;
 }

@@ -18,6 +18,7 @@ struct DevBatch {
     float2* Wf2;               // a V as (hi, lo) floats, tile-aligned per potential
     int32_t* counts;           // [n * n_trial]
     LevelWork* levels;         // [max_levels]
+    int32_t* fallback_list;    // [max_levels] slots handed to the bisection fallback
     int32_t max_levels;        // capacity of levels (n * level_capacity)
     int32_t level_capacity;    // slots per potential
     Header* hdr;
@@ -58,6 +59,12 @@ void launch_norm64(const DevBatch& b, int use_k, int sm_count, cudaStream_t s);
 void launch_write64(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_gather(const DevBatch& b, int32_t* n_total, int32_t* n_out, double* energy, int32_t* nodes,
                    int32_t* status, double* err_est, int apply_dE, cudaStream_t s);
+
+// polish.cu (fast method: compensated-FP32 recurrence, FP64 matching and norm)
+void launch_newton_df(const DevBatch& b, int sm_count, cudaStream_t s);
+void launch_norm_df(const DevBatch& b, int sm_count, cudaStream_t s);
+void launch_write_df(const DevBatch& b, int sm_count, cudaStream_t s);
+void launch_fallback_df(const DevBatch& b, int sm_count, cudaStream_t s);
 
 // adjoint.cu
 void launch_adjoint(const DevBatch& b, const double* dL_dE, double* dL_dV, int64_t total_points,

@@ -40,8 +40,9 @@ __device__ __forceinline__ bool cancelled(const DevBatch& b) { return b.cancel &
 // match points stay off the two boundary points (both sides non-empty)
 __device__ __forceinline__ int clamp_inner(const PotMeta& m, int k) { return max(m.i0 + 1, min(k, m.i1 - 1)); }
 
-// move the match point to the peak of |psi| when |psi| there is > 4x |psi_k|
-constexpr int kPeakLog2 = 3;
+// move the match point to the peak of |psi| when the sampled peak is at least
+// 2^kPeakLog2 (in binary exponent) above |psi_k|
+constexpr int kPeakLog2 = 2;
 
 // ------------------------------------------------------------------ FP64 pass
 
@@ -231,19 +232,29 @@ __device__ __forceinline__ Pass32 cooley32(const PotMeta& m, const float2* __res
         const int from = side == 0 ? m.i0 : m.i1;
         const int to = k;
         const int dir = side == 0 ? 1 : -1;
-        int s = 0, ecum = 0;
-        for (int i = from; i != to; i += dir) {
-            const float2 w = __ldg(Wf + i);
-            const float T = (aEh - w.x) + (aEl - w.y);
-            const float f = 1.0f + T;
-            S = fmaf(f * f, S, A * A);
-            const float X = fmaf(-12.0f, A, D);
-            D = fmaf(T, X, D);
-            const float An = A + fmaf(T, A, D);
-            nodes += (__float_as_uint(An) ^ __float_as_uint(A)) >> 31;
-            A = An;
-            if (++s == 16) {
-                s = 0;
+        int ecum = 0;
+        const int nsteps = (to - from) * dir;
+        // 8 loads in flight per thread: the grid values do not depend on the state
+        for (int base = 0; base < nsteps; base += 8) {
+            float2 w8[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) w8[u] = __ldg(Wf + from + dir * min(base + u, nsteps - 1));
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                if (base + u < nsteps) {
+                    const float2 w = w8[u];
+                    const float T = (aEh - w.x) + (aEl - w.y);
+                    const float f = 1.0f + T;
+                    S = fmaf(f * f, S, A * A);
+                    const float X = fmaf(-12.0f, A, D);
+                    D = fmaf(T, X, D);
+                    const float An = A + fmaf(T, A, D);
+                    nodes += (__float_as_uint(An) ^ __float_as_uint(A)) >> 31;
+                    A = An;
+                }
+            }
+            const int i = from + dir * min(base + 7, nsteps - 1);
+            {
                 const float mm = fmaxf(fabsf(A), fabsf(D));
                 const int e = ((__float_as_int(mm) >> 23) & 0xff) - 126;
                 if (mm > 0.0f && e > -60 && e < 60) {
@@ -288,11 +299,12 @@ __device__ __forceinline__ Pass32 cooley32(const PotMeta& m, const float2* __res
     return r;
 }
 
-// Safeguarded Cooley-Newton in FP32.  The match point is the outer turning
-// point unless |psi| stitched there peaks > 4x higher elsewhere (an inner-
-// well level of a double well), then that peak.  Every pass updates the count
-// bracket; a small Newton step is confirmed by a count on the far side of the
-// predicted root, otherwise the level continues by bisection.
+// Safeguarded Cooley-Newton in FP32.  The match point follows the peak of
+// |psi| (re-estimated from every pass: matching where the eigenvector is
+// largest keeps the correction quadratic; at a turning point where psi is small
+// it converges to a spurious point).  Every pass updates the count bracket; a
+// small Newton step is confirmed by a count on the far side of the predicted
+// root, otherwise the level continues by bisection.
 constexpr double kTol32 = 2e-9;
 
 __global__ void __launch_bounds__(kLevelThreads) refine32_kernel(DevBatch b) {
@@ -309,7 +321,7 @@ __global__ void __launch_bounds__(kLevelThreads) refine32_kernel(DevBatch b) {
         const double* W64 = b.W64 + m.off;
         double lo = w.lo, hi = w.hi, E = w.E;
         int k = clamp_inner(m, match_index(m, b.Msuf, E));
-        bool k_fixed = false, bisect = false, confirming = false, done = false;
+        bool bisect = false, confirming = false, done = false;
         double E_star = E, sum = 1.0;
         int it = 0;
         for (; it < 48; ++it) {
@@ -317,13 +329,8 @@ __global__ void __launch_bounds__(kLevelThreads) refine32_kernel(DevBatch b) {
             if (r.count > w.v) hi = E;
             else lo = E;
             sum = r.sum;
-            if (!k_fixed) {
-                k_fixed = true;
-                if (r.peak_log2 >= kPeakLog2) {  // redo at the same energy with the better match point
-                    k = clamp_inner(m, r.peak_i);
-                    continue;
-                }
-            }
+            const bool moved = r.peak_log2 >= kPeakLog2;
+            if (moved) k = clamp_inner(m, r.peak_i);
             if (confirming) {
                 confirming = false;
                 if (hi - lo <= 3.0 * kTol32 + 1e-15 && E_star >= lo && E_star <= hi) {
@@ -338,7 +345,7 @@ __global__ void __launch_bounds__(kLevelThreads) refine32_kernel(DevBatch b) {
                 break;
             }
             double En;
-            if (!bisect) {
+            if (!bisect && !moved) {
                 En = E + r.dE;
                 if (!(En > lo && En < hi) || !isfinite(En)) {
                     En = 0.5 * (lo + hi);
@@ -349,7 +356,7 @@ __global__ void __launch_bounds__(kLevelThreads) refine32_kernel(DevBatch b) {
                     confirming = true;
                 }
             } else {
-                En = 0.5 * (lo + hi);
+                En = 0.5 * (lo + hi);  // bisection (also after moving the match point)
             }
             E = En;
         }
@@ -367,11 +374,12 @@ __global__ void __launch_bounds__(kLevelThreads) refine32_kernel(DevBatch b) {
     }
 }
 
-// One FP64 Cooley correction from the FP32 energy at the FP32 match point,
-// with the FP32 sum psi~^2 as the Newton denominator (it only scales the step).
-// A correction inconsistent with the FP32 bracket or a stitched solution
-// with the wrong node count falls back to FP64 bisection on the scan bracket
-// widened by one trial spacing.
+// FP64 Cooley corrections from the FP32 energy at the FP32 match point, with
+// the FP32 sum psi~^2 as the Newton denominator (it only scales the step).
+// One pass is accepted when its step is as small as the FP32 stage allows
+// (quadratic convergence then leaves ~1e-13); otherwise up to three more
+// passes inside an FP64 count bracket, and FP64 bisection on the scan bracket
+// (widened by one trial spacing) as the last resort.
 __global__ void __launch_bounds__(kLevelThreads) newton64_kernel(DevBatch b) {
     const int total = b.hdr->total_levels;
     for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < total; slot += gridDim.x * blockDim.x) {
@@ -379,34 +387,43 @@ __global__ void __launch_bounds__(kLevelThreads) newton64_kernel(DevBatch b) {
         if (w.status & (EPSCU_STATUS_NOTFOUND | EPSCU_STATUS_CANCELLED)) continue;
         const PotMeta m = b.meta[w.p];
         const double* W = b.W64 + m.off;
-        int nodes = 0;
-        const double gamma = gamma64(m, W, w.E, w.k, nodes);
-        const double Tk = __dsub_rn(__dmul_rn(m.a, w.E), __ldg(W + w.k));
-        const double fk = 1.0 + Tk;
-        const double dE = gamma * fk * fk / (12.0 * m.a * w.norm_k_in);
-        const double En = w.E + dE;
-        const double slack = 4.0 * (w.hi - w.lo) + 1e-8;
-        if (nodes != w.v || !(fabs(dE) <= slack) || !isfinite(En)) {
-            const PotMeta mm = m;
-            const int j = (int)floor((w.E - mm.e_lo) / mm.delta);
-            double lo = fmax(mm.e_lo, mm.e_lo + (j - 1) * mm.delta), hi = fmin(mm.e_cap, mm.e_lo + (j + 2) * mm.delta);
+        double E = w.E;
+        double lo64 = w.lo - 1e-8, hi64 = w.hi + 1e-8;
+        bool ok = false;
+        for (int it = 0; it < 4 && !ok; ++it) {
+            int nodes = 0;
+            const double gamma = gamma64(m, W, E, w.k, nodes);
+            const double Tk = __dsub_rn(__dmul_rn(m.a, E), __ldg(W + w.k));
+            const double fk = 1.0 + Tk;
+            const double dE = gamma * fk * fk / (12.0 * m.a * w.norm_k_in);
+            const int count = nodes + (gamma < 0.0 ? 1 : 0);
+            if (count > w.v) hi64 = fmin(hi64, E);
+            else lo64 = fmax(lo64, E);
+            const double En = E + dE;
+            if (!isfinite(En) || !(En >= lo64 && En <= hi64) || nodes != w.v) break;
+            const bool small = fabs(dE) <= (it == 0 ? 1e-8 : 1e-12 * fmax(1.0, fabs(E)));
+            E = En;
+            ok = small;
+        }
+        if (!ok) {
+            const int j = (int)floor((w.E - m.e_lo) / m.delta);
+            double lo = fmax(m.e_lo, m.e_lo + (j - 1) * m.delta), hi = fmin(m.e_cap, m.e_lo + (j + 2) * m.delta);
             atomicAdd(&b.hdr->fallbacks, 1);
-            for (int itb = 0; itb < mm.n_bisect + 3; ++itb) {
+            for (int itb = 0; itb < m.n_bisect + 3; ++itb) {
                 const double mid = __dmul_rn(0.5, __dadd_rn(lo, hi));
-                if (count64(mm, W, mid, w.k) > w.v) hi = mid;
+                if (count64(m, W, mid, w.k) > w.v) hi = mid;
                 else lo = mid;
             }
-            w.E = __dmul_rn(0.5, __dadd_rn(lo, hi));
-        } else {
-            w.E = En;
+            E = __dmul_rn(0.5, __dadd_rn(lo, hi));
         }
+        w.E = E;
         b.levels[slot] = w;
     }
 }
 
 // use_k: keep the match point chosen by the FP32 refinement (fast method);
-// otherwise the outer turning point, moved to the peak of |psi| when the
-// solution stitched there peaks more than 4x higher elsewhere (as the oracle).
+// otherwise the outer turning point, moved to the peak of |psi| of the solution
+// stitched there (as the oracle's match point).
 __global__ void __launch_bounds__(kLevelThreads) norm64_kernel(DevBatch b, int use_k) {
     const int total = b.hdr->total_levels;
     for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < total; slot += gridDim.x * blockDim.x) {
@@ -415,7 +432,7 @@ __global__ void __launch_bounds__(kLevelThreads) norm64_kernel(DevBatch b, int u
         const PotMeta m = b.meta[w.p];
         int k = use_k ? w.k : clamp_inner(m, match_index(m, b.Msuf, w.E));
         Pass64 r = cooley64<true>(m, b.W64 + m.off, w.E, k);
-        if (!use_k && r.peak_log2 >= kPeakLog2) {
+        if (!use_k && r.peak_log2 >= 1) {
             k = clamp_inner(m, r.peak_i);
             r = cooley64<true>(m, b.W64 + m.off, w.E, k);
         }

@@ -1,0 +1,329 @@
+// polish.cu -- final passes of the fast method in compensated FP32.
+//
+// The recurrence of the last passes runs in double-float arithmetic (~48-bit
+// significands, see dfloat.cuh) in the Blatt difference form
+//     D' = D + T (D - 12 A),   A' = A + (T A + D')
+// with T = aE - W carried as a double-float pair; FP64 is used only for the
+// matching-point difference gamma_k, the Newton step and the norm integral
+// (sum psi^2, accumulated in FP64 every 8 points).  Per grid point this costs
+// ~110 FP32 instructions and at most one FP64 instruction, against ~16 FP64
+// instructions (~1000 FP32-issue equivalents on GB300) for the same pass in
+// native FP64.
+//
+//  newton_df : Cooley corrections from the FP32 energy (1..4 passes) inside an
+//              FP64 count bracket; levels that do not settle go to
+//  fallback_df: bisection on compensated-FP32 counts, one level per warp.
+//  norm_df   : sums, node count, peak of |psi| and the constants of the write.
+//  write_df  : recomputes the pass and writes psi (FP64) to HBM.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "dfloat.cuh"
+#include "launch.h"
+
+namespace epscu {
+
+namespace {
+
+constexpr int kThreads = 128;
+
+__device__ __forceinline__ int clamp_k(const PotMeta& m, int k) { return max(m.i0 + 1, min(k, m.i1 - 1)); }
+
+// MODE 0: state only (Newton)   MODE 1: + sums, psi-hat, peak   MODE 2: + write
+template <int MODE>
+struct SideDF {
+    dfl A, D, q;      // state ~ s (u_i, u_i - u_{i-1}); q = 1/s (MODE >= 1)
+    int eA, eQ;       // exponents removed from (A, D) and from q
+    int nodes;
+    double S;         // MODE 1: sum of psi-hat^2 in the current stored scale (FP64)
+    int peak_L, peak_i;
+};
+
+template <int MODE>
+__device__ __forceinline__ void side_df(const float2* __restrict__ Wf, dfl aE, int from, int to, int dir,
+                                        SideDF<MODE>& st, double* __restrict__ out, double L, int Xk) {
+    st.A = {1.0f, 0.0f};
+    st.D = {1.0f, 0.0f};  // u_from = 1, u_{from-dir} = 0
+    st.q = {1.0f, 0.0f};
+    st.eA = st.eQ = 0;
+    st.nodes = 0;
+    st.S = 0.0;
+    st.peak_L = -(1 << 30);
+    st.peak_i = from;
+    dfl Sacc = {0.0f, 0.0f};
+    dfl F = {0.0f, 0.0f};
+    if (MODE == 2) F = df_from_double(L * ldexp(1.0, min(1000, max(-1100, -Xk))));
+    const int nsteps = (to - from) * dir;
+    for (int base = 0; base < nsteps; base += 8) {
+        float2 w8[8];  // 8 grid values in flight: they do not depend on the state
+#pragma unroll
+        for (int u = 0; u < 8; ++u) w8[u] = __ldg(Wf + from + dir * min(base + u, nsteps - 1));
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            if (base + u >= nsteps) break;
+            const int i = from + dir * (base + u);
+            const float2 w = w8[u];
+            dfl T = two_sum(aE.h, -w.x);
+            T = fast_two_sum(T.h, __fadd_rn(T.l, __fsub_rn(aE.l, w.y)));
+            if (MODE >= 1) {
+                const dfl f = df_add({1.0f, 0.0f}, T);
+                const dfl qn = df_mul(st.q, df_recip(f));
+                const dfl psi = df_mul(st.A, qn);  // psi-hat_i = A_i / s_{i+1}
+                if (MODE == 1) {
+                    const float p = __fmul_rn(psi.h, psi.h);
+                    const float e = __fmaf_rn(psi.h, psi.h, -p);
+                    Sacc = df_add(Sacc, {p, __fmaf_rn(2.0f * psi.h, psi.l, e)});
+                } else {
+                    const dfl v = df_mul(psi, F);
+                    out[i] = f2d(v.h) + f2d(v.l);
+                }
+                st.q = qn;
+            }
+            const dfl X = df_add(st.D, df_mulf(st.A, -12.0f));
+            st.D = df_add(st.D, df_mul(T, X));
+            const dfl An = df_add(st.A, df_add(df_mul(T, st.A), st.D));
+            st.nodes += (__float_as_uint(An.h) ^ __float_as_uint(st.A.h)) >> 31;
+            st.A = An;
+        }
+        // renormalise every 8 steps (exact powers of two)
+        const int i = from + dir * min(base + 7, nsteps - 1);
+        const float mm = fmaxf(fabsf(st.A.h), fabsf(st.D.h));
+        int e = 0, eq = 0;
+        if (mm > 0.0f && mm < INFINITY) {
+            e = max(-120, min(120, fexp(mm)));
+            const float sc = fpow2(-e);
+            st.A = df_scale(st.A, sc);
+            st.D = df_scale(st.D, sc);
+            st.eA += e;
+        }
+        if (MODE >= 1) {
+            eq = max(-120, min(120, fexp(st.q.h)));
+            st.q = df_scale(st.q, fpow2(-eq));
+            st.eQ += eq;
+            if (MODE == 1) {
+                // flush the block sum into FP64 in the old scale, then rescale
+                st.S = (st.S + (f2d(Sacc.h) + f2d(Sacc.l))) * ldexp(1.0, -2 * (e + eq));
+                Sacc = {0.0f, 0.0f};
+                const float mag = fabsf(__fmul_rn(st.A.h, st.q.h));
+                if (mag > 0.0f) {
+                    const int Lm = fexp(mag) + st.eA + st.eQ;
+                    if (Lm > st.peak_L) {
+                        st.peak_L = Lm;
+                        st.peak_i = i;
+                    }
+                }
+            } else if (e + eq != 0) {
+                F = df_from_double(L * ldexp(1.0, min(1000, max(-1100, st.eA + st.eQ - Xk))));
+            }
+        }
+    }
+    if (MODE == 1) st.S += f2d(Sacc.h) + f2d(Sacc.l);
+}
+
+__device__ __forceinline__ dfl energy_df(const PotMeta& m, double E) {
+    return df_from_double(__dmul_rn(m.a, E));
+}
+
+struct PassDF {
+    double dE, gamma, sum;
+    double pk_out, pk_in;
+    int ex_out, ex_in;
+    int nodes, count;
+    int peak_i, peak_log2;
+};
+
+// one pass at E with match point k; MODE 0: gamma/count only, MODE 1: + sums
+template <int MODE>
+__device__ PassDF pass_df(const PotMeta& m, const float2* __restrict__ Wf, const double* __restrict__ W64, double E,
+                          int k, double sum_fallback) {
+    const dfl aE = energy_df(m, E);
+    SideDF<MODE> o, in;
+    side_df<MODE>(Wf, aE, m.i0, k, +1, o, nullptr, 0.0, 0);
+    side_df<MODE>(Wf, aE, m.i1, k, -1, in, nullptr, 0.0, 0);
+    const double Tk = __dsub_rn(__dmul_rn(m.a, E), __ldg(W64 + k));
+    const double fk = 1.0 + Tk;
+    const double Ao = df_to_double(o.A), Do = df_to_double(o.D);
+    const double Ai = df_to_double(in.A), Di = df_to_double(in.D);
+    PassDF r;
+    // gamma_k = -12 T_k / f_k + D_o / u_k + D_i / v_k in FP64 (no cancellation)
+    r.gamma = -12.0 * Tk / fk + Do / Ao + Di / Ai;
+    r.nodes = o.nodes + in.nodes;
+    r.count = r.nodes + (r.gamma < 0.0 ? 1 : 0);
+    r.peak_i = k;
+    r.peak_log2 = 0;
+    r.pk_out = r.pk_in = 0.0;
+    r.ex_out = r.ex_in = 0;
+    if (MODE == 1) {
+        // psi-hat at k from each side: A_k q_k / f_k
+        const double rfk = 1.0 / fk;
+        r.pk_out = Ao * df_to_double(o.q) * rfk;
+        r.pk_in = Ai * df_to_double(in.q) * rfk;
+        r.ex_out = o.eA + o.eQ;
+        r.ex_in = in.eA + in.eQ;
+        r.sum = o.S / (r.pk_out * r.pk_out) + in.S / (r.pk_in * r.pk_in) + 1.0;
+        const int Lo = (r.pk_out != 0.0 ? exp_of(fabs(r.pk_out)) : -1000) + r.ex_out;
+        const int Li = (r.pk_in != 0.0 ? exp_of(fabs(r.pk_in)) : -1000) + r.ex_in;
+        const int po = o.peak_L - Lo, pi = in.peak_L - Li;
+        r.peak_log2 = max(po, pi);
+        r.peak_i = po >= pi ? o.peak_i : in.peak_i;
+    } else {
+        r.sum = sum_fallback;
+    }
+    r.dE = r.gamma * fk * fk / (12.0 * m.a * r.sum);
+    return r;
+}
+
+__global__ void __launch_bounds__(kThreads) newton_df_kernel(DevBatch b) {
+    const int total = b.hdr->total_levels;
+    for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < total; slot += gridDim.x * blockDim.x) {
+        LevelWork w = b.levels[slot];
+        if (w.status & (EPSCU_STATUS_NOTFOUND | EPSCU_STATUS_CANCELLED)) continue;
+        const PotMeta m = b.meta[w.p];
+        const float2* Wf = b.Wf2 + m.offf;
+        const double* W = b.W64 + m.off;
+        double E = w.E;
+        double lo = w.lo - 1e-8, hi = w.hi + 1e-8;
+        bool ok = false;
+        for (int it = 0; it < 4 && !ok; ++it) {
+            const PassDF r = pass_df<0>(m, Wf, W, E, w.k, w.norm_k_in);
+            if (r.count > w.v) hi = fmin(hi, E);
+            else lo = fmax(lo, E);
+            const double En = E + r.dE;
+            if (!isfinite(En) || !(En >= lo && En <= hi) || r.nodes != w.v) break;
+            ok = fabs(r.dE) <= 1e-12 * fmax(1.0, fabs(E));
+            E = En;
+        }
+        if (!ok) {
+            // hand the level to the bisection fallback kernel (so this warp
+            // does not stall on it)
+            w.status |= EPSCU_STATUS_FALLBACK;
+            const int q = atomicAdd(&b.hdr->fallbacks, 1);
+            if (q < b.max_levels) b.fallback_list[q] = slot;
+        } else {
+            w.E = E;
+        }
+        b.levels[slot] = w;
+    }
+}
+
+// Bisection on compensated-FP32 twisted Sturm counts for the levels the Newton
+// stage could not settle (near-degenerate pairs, match points across a
+// barrier).  The FP32 bracket widened by 2e-8 is verified by counts at both
+// ends first; the scan bracket (widened by one trial spacing) is the fallback.
+// One level per warp (lane 0): the list is short and each level is serial.
+__global__ void __launch_bounds__(32) fallback_df_kernel(DevBatch b) {
+    const int n = min(b.hdr->fallbacks, b.max_levels);
+    if (threadIdx.x != 0) return;
+    for (int q = blockIdx.x; q < n; q += gridDim.x) {
+        const int slot = b.fallback_list[q];
+        LevelWork w = b.levels[slot];
+        const PotMeta m = b.meta[w.p];
+        const float2* Wf = b.Wf2 + m.offf;
+        const double* W = b.W64 + m.off;
+        auto count_at = [&](double E) { return pass_df<0>(m, Wf, W, E, w.k, 1.0).count; };
+        double lo = fmax(m.e_lo, w.lo - 2e-8), hi = fmin(m.e_cap, w.hi + 2e-8);
+        if (!(count_at(lo) <= w.v && count_at(hi) > w.v)) {
+            lo = fmax(m.e_lo, w.lo0 - m.delta);
+            hi = fmin(m.e_cap, w.hi0 + m.delta);
+        }
+        for (int it = 0; it < 64; ++it) {
+            if (hi - lo <= 1e-12 * fmax(1.0, fabs(lo))) break;
+            const double mid = 0.5 * (lo + hi);
+            if (!(mid > lo && mid < hi)) break;
+            if (count_at(mid) > w.v) hi = mid;
+            else lo = mid;
+        }
+        w.E = 0.5 * (lo + hi);
+        w.lo = lo;
+        w.hi = hi;
+        w.status &= ~EPSCU_STATUS_FALLBACK;
+        b.levels[slot] = w;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) norm_df_kernel(DevBatch b) {
+    const int total = b.hdr->total_levels;
+    for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < total; slot += gridDim.x * blockDim.x) {
+        LevelWork w = b.levels[slot];
+        if (w.status & (EPSCU_STATUS_NOTFOUND | EPSCU_STATUS_CANCELLED)) continue;
+        const PotMeta m = b.meta[w.p];
+        const float2* Wf = b.Wf2 + m.offf;
+        const double* W = b.W64 + m.off;
+        // match point candidates: the FP32 one, the peak of |psi| seen by this
+        // pass, the outer turning point and its peak; the first whose
+        // stitched solution has v nodes wins
+        int k = w.k;
+        PassDF r = pass_df<1>(m, Wf, W, w.E, k, 1.0);
+        if (r.peak_log2 >= 1) {
+            k = clamp_k(m, r.peak_i);
+            r = pass_df<1>(m, Wf, W, w.E, k, 1.0);
+        }
+        if (r.nodes != w.v) {
+            const int kt = clamp_k(m, match_index(m, b.Msuf, w.E));
+            PassDF r2 = pass_df<1>(m, Wf, W, w.E, kt, 1.0);
+            int k2 = kt;
+            if (r2.nodes != w.v && r2.peak_log2 >= 1) {
+                k2 = clamp_k(m, r2.peak_i);
+                r2 = pass_df<1>(m, Wf, W, w.E, k2, 1.0);
+            }
+            if (r2.nodes == w.v) {
+                r = r2;
+                k = k2;
+            }
+        }
+        double ck = 1.0 / sqrt(m.h * r.sum);
+        if (r.pk_out < 0.0) ck = -ck;  // psi > 0 next to the inner wall
+        w.k = k;
+        w.ck = ck;
+        w.norm_k_out = ck / r.pk_out;
+        w.norm_k_in = ck / r.pk_in;
+        w.ex_out = r.ex_out;
+        w.ex_in = r.ex_in;
+        w.dE = r.dE;
+        w.nodes = r.nodes;
+        if (!isfinite(r.dE) || !isfinite(ck)) w.status |= EPSCU_STATUS_NONFINITE;
+        if (r.nodes != w.v && !(m.status & EPSCU_STATUS_UNDER)) w.status |= EPSCU_STATUS_NOTFOUND;
+        b.levels[slot] = w;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) write_df_kernel(DevBatch b) {
+    const int total = b.hdr->total_levels;
+    if (!b.psi || b.hdr->error) return;
+    for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < total; slot += gridDim.x * blockDim.x) {
+        const LevelWork w = b.levels[slot];
+        const PotMeta m = b.meta[w.p];
+        double* out = b.psi + m.psi_off + (int64_t)(w.v - b.min_level) * m.N;
+        for (int i = 0; i < m.i0; ++i) out[i] = 0.0;
+        for (int i = m.i1 + 1; i < m.N; ++i) out[i] = 0.0;
+        if (w.status & (EPSCU_STATUS_NOTFOUND | EPSCU_STATUS_CANCELLED | EPSCU_STATUS_NONFINITE)) {
+            for (int i = m.i0; i <= m.i1; ++i) out[i] = 0.0;
+            continue;
+        }
+        const float2* Wf = b.Wf2 + m.offf;
+        const dfl aE = energy_df(m, w.E);
+        SideDF<2> st;
+        side_df<2>(Wf, aE, m.i0, w.k, +1, st, out, w.norm_k_out, w.ex_out);
+        side_df<2>(Wf, aE, m.i1, w.k, -1, st, out, w.norm_k_in, w.ex_in);
+        out[w.k] = w.ck;
+    }
+}
+
+}  // namespace
+
+void launch_newton_df(const DevBatch& b, int sm_count, cudaStream_t s) {
+    newton_df_kernel<<<sm_count * 8, kThreads, 0, s>>>(b);
+}
+void launch_norm_df(const DevBatch& b, int sm_count, cudaStream_t s) {
+    norm_df_kernel<<<sm_count * 8, kThreads, 0, s>>>(b);
+}
+void launch_write_df(const DevBatch& b, int sm_count, cudaStream_t s) {
+    write_df_kernel<<<sm_count * 8, kThreads, 0, s>>>(b);
+}
+void launch_fallback_df(const DevBatch& b, int sm_count, cudaStream_t s) {
+    fallback_df_kernel<<<sm_count * 4, 32, 0, s>>>(b);
+}
+
+}  // namespace epscu

@@ -247,6 +247,8 @@ __global__ void bracket_kernel(DevBatch b) {
             w.hi = trial_energy(m, lo);
             w.E = __dmul_rn(0.5, __dadd_rn(w.lo, w.hi));
         }
+        w.lo0 = w.lo;
+        w.hi0 = w.hi;
         b.levels[m.level_base + s] = w;
     }
 }

@@ -136,6 +136,71 @@ __device__ __forceinline__ void step32(float aEh, float aEl, float2 w, float& A,
     A = An;
 }
 
+// Step with the sign of A shifted into a bit history (one funnel shift per
+// step; the sign changes are popcounted once per 16-step chunk).
+__device__ __forceinline__ void step32b(float aEh, float aEl, float wx, float wy, float& A, float& D, uint32_t& bits) {
+    const float T = (aEh - wx) + (aEl - wy);
+    const float X = fmaf(-12.0f, A, D);
+    D = fmaf(T, X, D);
+    A = A + fmaf(T, A, D);
+    bits = __funnelshift_l(__float_as_uint(A), bits, 1);
+}
+
+__device__ __forceinline__ void flush_bits(uint32_t& bits, int& nodes) {
+    nodes += __popc((bits ^ (bits >> 1)) & 0xffffu);
+    bits &= 1u;
+}
+
+// 16 ascending points starting at a 16-aligned offset of the tile
+__device__ __forceinline__ void chunk16_up(const float2* __restrict__ c, float aEh, float aEl, float& A, float& D,
+                                           uint32_t& bits, int& nodes) {
+    const float4* q4 = reinterpret_cast<const float4*>(c);
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+        const float4 q = q4[u];
+        step32b(aEh, aEl, q.x, q.y, A, D, bits);
+        step32b(aEh, aEl, q.z, q.w, A, D, bits);
+    }
+    flush_bits(bits, nodes);
+    renorm_f(A, D);
+}
+
+// the same 16 points descending
+__device__ __forceinline__ void chunk16_down(const float2* __restrict__ c, float aEh, float aEl, float& A, float& D,
+                                             uint32_t& bits, int& nodes) {
+    const float4* q4 = reinterpret_cast<const float4*>(c);
+#pragma unroll
+    for (int u = 7; u >= 0; --u) {
+        const float4 q = q4[u];
+        step32b(aEh, aEl, q.z, q.w, A, D, bits);
+        step32b(aEh, aEl, q.x, q.y, A, D, bits);
+    }
+    flush_bits(bits, nodes);
+    renorm_f(A, D);
+}
+
+// points a0..a1 (a0 <= a1) of tile tb (first point T0), ascending
+__device__ __forceinline__ void run_up(const float2* __restrict__ tb, int T0, int a0, int a1, float aEh, float aEl,
+                                       float& A, float& D, int& nodes) {
+    int i = a0;
+    for (; i <= a1 && (i & 15); ++i) step32(aEh, aEl, tb[i - T0], A, D, nodes);
+    renorm_f(A, D);
+    uint32_t bits = __float_as_uint(A) >> 31;
+    for (; i + 15 <= a1; i += 16) chunk16_up(tb + (i - T0), aEh, aEl, A, D, bits, nodes);
+    for (; i <= a1; ++i) step32(aEh, aEl, tb[i - T0], A, D, nodes);
+}
+
+// points a0..a1 (a0 >= a1) of tile tb, descending
+__device__ __forceinline__ void run_down(const float2* __restrict__ tb, int T0, int a0, int a1, float aEh, float aEl,
+                                         float& A, float& D, int& nodes) {
+    int i = a0;
+    for (; i >= a1 && ((i & 15) != 15); --i) step32(aEh, aEl, tb[i - T0], A, D, nodes);
+    renorm_f(A, D);
+    uint32_t bits = __float_as_uint(A) >> 31;
+    for (; i - 15 >= a1; i -= 16) chunk16_down(tb + (i - 15 - T0), aEh, aEl, A, D, bits, nodes);
+    for (; i >= a1; --i) step32(aEh, aEl, tb[i - T0], A, D, nodes);
+}
+
 template <int THREADS, int TILE, int STAGES>
 __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, int n_items) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -194,7 +259,6 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
         float A = 1.0f, D = 1.0f;  // u_{i0} = 1, u_{i0-1} = 0
         float Ao = 1.0f, Do = 1.0f;
         int nodes = 0;
-        int steps = 0;
         bool inward = false;
 
         for (int t = 0; t < L; ++t) {
@@ -208,10 +272,7 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
             const int T0 = seq.tile(t) * TILE;
             if (t < seq.n_out) {
                 const int a0 = max(m.i0, T0), a1 = min(k - 1, T0 + TILE - 1);
-                for (int i = a0; i <= a1; ++i) {
-                    step32(aEh, aEl, tb[i - T0], A, D, nodes);
-                    if ((++steps & 15) == 0) renorm_f(A, D);
-                }
+                run_up(tb, T0, a0, a1, aEh, aEl, A, D, nodes);
             } else {
                 if (!inward) {
                     inward = true;
@@ -219,13 +280,9 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
                     Do = D;
                     A = 1.0f;  // v_{i1} = 1, v_{i1+1} = 0
                     D = 1.0f;
-                    steps = 0;
                 }
                 const int a0 = min(m.i1, T0 + TILE - 1), a1 = max(k + 1, T0);
-                for (int i = a0; i >= a1; --i) {
-                    step32(aEh, aEl, tb[i - T0], A, D, nodes);
-                    if ((++steps & 15) == 0) renorm_f(A, D);
-                }
+                run_down(tb, T0, a0, a1, aEh, aEl, A, D, nodes);
             }
             __syncthreads();  // every thread is done with stage st
             if (s_abort) {

@@ -94,7 +94,9 @@ typedef struct epscu_opts {
     int32_t method;      /* EPSCU_METHOD_* */
     int32_t flags;       /* EPSCU_MEM_DEVICE | EPSCU_WANT_PSI */
     double tol;          /* bisection width of the plain method (default 1e-12) */
-    void* stream;        /* cudaStream_t to run on; NULL = the context's stream */
+    void* stream;        /* cudaStream_t the inputs are ordered on and the outputs are
+                            ordered back to (NULL: the legacy default stream); the work
+                            itself runs on the context's stream */
     int32_t tune;        /* 0 = use cached/default launch shape, 1 = autotune */
     int32_t reserved;
 } epscu_opts;

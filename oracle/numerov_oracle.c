@@ -235,17 +235,17 @@ static int32_t clamp_inner(const eo_grid* g, int32_t k) {
     return k;
 }
 
-/* Robust match point: the outer classical turning point (kept off the two
- * boundary points), unless the wavefunction stitched there peaks more than 4
- * times higher elsewhere (a level living in an inner well of a double well,
- * or a turning point beyond the cut-off grid), then that peak. */
+/* Match point: the peak of |psi| of the solution stitched at the outer
+ * classical turning point, kept off the two boundary points.  Matching where
+ * the eigenvector is largest keeps Cooley's correction in its quadratic regime
+ * (at a turning point where psi is small -- inner-well levels of a double
+ * well, turning points beyond a cut-off grid -- it is not). */
 int32_t eo_match_point(const double* V, const eo_grid* g, double E) {
     const int32_t k = clamp_inner(g, eo_match_index(V, g, E));
     double* tmp = (double*)malloc(sizeof(double) * (size_t)g->N);
-    double ratio = 1.0;
-    const int32_t m = wavefunction_k(V, g, E, k, tmp, &ratio);
+    const int32_t m = wavefunction_k(V, g, E, k, tmp, NULL);
     free(tmp);
-    return ratio > 4.0 ? clamp_inner(g, m) : k;
+    return clamp_inner(g, m);
 }
 
 void eo_wavefunction(const double* V, const eo_grid* g, double E, double* psi) {

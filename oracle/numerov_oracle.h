@@ -96,10 +96,9 @@ int32_t eo_count(const double* V, const eo_grid* g, double E, int32_t k);
  * k_scan when there is none. */
 int32_t eo_match_index(const double* V, const eo_grid* g, double E);
 
-/* Match point used for wavefunctions and Cooley corrections: the outer
- * turning point (clamped to i0+1..i1-1), or the peak of |psi| when the
- * solution stitched at the turning point peaks more than 4x higher elsewhere
- * (inner-well levels, turning points beyond a cut-off grid). */
+/* Match point used for wavefunctions and Cooley corrections: the peak of
+ * |psi| of the solution stitched at the outer turning point (clamped to
+ * i0+1..i1-1). */
 int32_t eo_match_point(const double* V, const eo_grid* g, double E);
 
 /* One Cooley pass at E (match point k, or eo_match_point): returns the Newton
