@@ -83,18 +83,37 @@ class Solver:
         o = capi.Opts(int(g.method), capi.MEM_DEVICE | capi.WANT_PSI, 1e-12,
                       C.c_void_p(torch.cuda.current_stream(dev).cuda_stream), 0, 0)
         capi._check(self.ctx._lib.epscu_solve(self.ctx.handle, C.byref(b), C.byref(r), C.byref(o)))
-        self.psi, self.grids, self.total = psi, g, g.total
         mask = torch.arange(cap, device=dev)[None, :] < self.n_out[:, None].long()
         E = torch.where(mask, E, torch.zeros_like(E))
+        # everything the adjoint of this solve needs, independent of later solves
+        self.last = SolveRecord(g, psi, psi_off.copy(), self.n_out.cpu().numpy().astype(np.int32))
         return E, nodes, status, mask
 
-    def adjoint(self, gE: torch.Tensor) -> torch.Tensor:
+    def adjoint(self, gE: torch.Tensor, rec: "SolveRecord | None" = None) -> torch.Tensor:
+        """dL/dV of a recorded solve (default: this solver's last one)."""
+        rec = rec or self.last
+        g = rec.grids
         gE = gE.to(torch.float64).contiguous()
-        gV = torch.zeros(self.total, dtype=torch.float64, device=gE.device)
+        gV = torch.zeros(g.total, dtype=torch.float64, device=gE.device)
+        keep = [np.ascontiguousarray(x) for x in (g.offsets, g.N.astype(np.int32), g.r_min, g.r_max, rec.n_out,
+                                                   rec.psi_offsets)]
+        off, N, r0, r1, no, po = keep
         o = capi.Opts(0, capi.MEM_DEVICE, 0.0, C.c_void_p(torch.cuda.current_stream(gE.device).cuda_stream), 0, 0)
-        capi._check(self.ctx._lib.epscu_adjoint(self.ctx.handle, C.cast(C.c_void_p(gE.data_ptr()), capi._dp),
-                                                C.cast(C.c_void_p(gV.data_ptr()), capi._dp), 0, C.byref(o)))
+        capi._check(self.ctx._lib.epscu_adjoint_psi(
+            self.ctx.handle, int(N.size), capi._l(off), capi._i(N), capi._d(r0), capi._d(r1), capi._i(no),
+            int(g.capacity), C.cast(C.c_void_p(rec.psi.data_ptr()), capi._dp), capi._l(po),
+            C.cast(C.c_void_p(gE.data_ptr()), capi._dp), C.cast(C.c_void_p(gV.data_ptr()), capi._dp), C.byref(o)))
         return gV
+
+
+@dataclass
+class SolveRecord:
+    """Wavefunctions and layout of one solve (kept by autograd for its backward)."""
+
+    grids: Grids
+    psi: torch.Tensor
+    psi_offsets: np.ndarray
+    n_out: np.ndarray
 
 
 class LevelEnergies(torch.autograd.Function):
@@ -104,12 +123,13 @@ class LevelEnergies(torch.autograd.Function):
     def forward(ctx, V: torch.Tensor, grids: Grids, solver: Solver):
         E, nodes, status, mask = solver.solve(V.detach().contiguous(), grids)
         ctx.solver = solver
+        ctx.record = solver.last
         ctx.mark_non_differentiable(mask)
         return E, mask
 
     @staticmethod
     def backward(ctx, gE, gmask):
-        return ctx.solver.adjoint(gE), None, None
+        return ctx.solver.adjoint(gE, ctx.record), None, None
 
 
 def levels(V: torch.Tensor, grids: Grids, solver: Solver | None = None):

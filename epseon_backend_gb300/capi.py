@@ -121,6 +121,7 @@ EXPORTED = [
     "epscu_set_arena_block",
     "epscu_solve",
     "epscu_adjoint",
+    "epscu_adjoint_psi",
     "epscu_tabulate",
     "epscu_cancel",
     "epscu_last_stats",
@@ -159,6 +160,8 @@ def load(build_if_missing: bool = True):
     L.epscu_set_arena_block.argtypes = [C.c_void_p, C.c_int64]
     L.epscu_solve.argtypes = [C.c_void_p, C.POINTER(Batch), C.POINTER(Result), C.POINTER(Opts)]
     L.epscu_adjoint.argtypes = [C.c_void_p, _dp, _dp, C.c_int32, C.POINTER(Opts)]
+    L.epscu_adjoint_psi.argtypes = [C.c_void_p, C.c_int32, _lp, _ip, _dp, _dp, _ip, C.c_int32, _dp, _lp, _dp, _dp,
+                                    C.POINTER(Opts)]
     L.epscu_tabulate.argtypes = [C.c_void_p, C.c_int32, _ip, _dp, _lp, _ip, _dp, _dp, C.c_int32, _dp, C.POINTER(Opts)]
     L.epscu_cancel.argtypes = [C.c_void_p]
     L.epscu_last_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]

@@ -45,7 +45,34 @@ __global__ void adjoint_kernel(DevBatch b, const double* __restrict__ gE, double
     else gV[offsets[p] + i] = acc;
 }
 
+// Explicit layout (stateless adjoint): per-potential arrays on the device.
+__global__ void adjoint_explicit_kernel(int32_t cap, const int64_t* __restrict__ offsets, const int32_t* __restrict__ Ns,
+                                        const double* __restrict__ hs, const int32_t* __restrict__ n_outs,
+                                        const int64_t* __restrict__ psi_offs, const double* __restrict__ psi,
+                                        const double* __restrict__ gE, double* __restrict__ gV) {
+    const int p = blockIdx.y;
+    const int N = Ns[p];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const int n_out = n_outs[p];
+    const double* rows = psi + psi_offs[p] + i;
+    const double* g = gE + (int64_t)p * cap;
+    double acc = 0.0;
+    for (int s = 0; s < n_out; ++s) {
+        const double v = __ldg(rows + (int64_t)s * N);
+        acc = fma(g[s] * v, v, acc);
+    }
+    gV[offsets[p] + i] = acc * hs[p];
+}
+
 }  // namespace
+
+void launch_adjoint_explicit(int32_t n, int32_t cap, int32_t max_N, const int64_t* offsets, const int32_t* N,
+                             const double* h, const int32_t* n_out, const int64_t* psi_off, const double* psi,
+                             const double* gE, double* gV, cudaStream_t s) {
+    dim3 grid((max_N + 255) / 256, n);
+    adjoint_explicit_kernel<<<grid, 256, 0, s>>>(cap, offsets, N, h, n_out, psi_off, psi, gE, gV);
+}
 
 void launch_adjoint(const DevBatch& b, const double* dL_dE, double* dL_dV, int64_t total_points,
                     const int64_t* offsets_dev, int recompute, int sm_count, cudaStream_t s) {

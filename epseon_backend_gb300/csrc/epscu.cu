@@ -674,6 +674,68 @@ extern "C" epscu_status epscu_adjoint(epscu_ctx* ctx, const double* dL_dE, doubl
     return EPSCU_OK;
 }
 
+extern "C" epscu_status epscu_adjoint_psi(epscu_ctx* ctx, int32_t n, const int64_t* offsets, const int32_t* N,
+                                          const double* r_min, const double* r_max, const int32_t* n_out,
+                                          int32_t cap, const double* psi, const int64_t* psi_offsets,
+                                          const double* dL_dE, double* dL_dV, const epscu_opts* opts_in) {
+    if (!ctx || n <= 0 || cap <= 0 || !offsets || !N || !r_min || !r_max || !n_out || !psi || !psi_offsets ||
+        !dL_dE || !dL_dV)
+        return fail(EPSCU_ERR_INVALID, "bad arguments");
+    epscu_opts opts{};
+    if (opts_in) opts = *opts_in;
+    std::lock_guard<std::mutex> guard(ctx->mu);
+    cudaSetDevice(ctx->device);
+    const bool dev = (opts.flags & EPSCU_MEM_DEVICE) != 0;
+    std::vector<double> h(n);
+    int64_t total = 0, psi_total = 0;
+    int32_t max_N = 0;
+    for (int p = 0; p < n; ++p) {
+        if (N[p] < 2 || n_out[p] < 0 || n_out[p] > cap) return fail(EPSCU_ERR_INVALID, "bad N or n_out");
+        h[p] = (r_max[p] - r_min[p]) / (double)(N[p] - 1);
+        total = std::max<int64_t>(total, offsets[p] + N[p]);
+        psi_total = std::max<int64_t>(psi_total, psi_offsets[p] + (int64_t)n_out[p] * N[p]);
+        max_N = std::max(max_N, N[p]);
+    }
+    cudaError_t ce = cudaSuccess;
+    auto* d_off = (int64_t*)ctx->get("adjx_off", sizeof(int64_t) * n, &ce);
+    auto* d_N = (int32_t*)ctx->get("adjx_N", sizeof(int32_t) * n, &ce);
+    auto* d_h = (double*)ctx->get("adjx_h", sizeof(double) * n, &ce);
+    auto* d_no = (int32_t*)ctx->get("adjx_no", sizeof(int32_t) * n, &ce);
+    auto* d_po = (int64_t*)ctx->get("adjx_po", sizeof(int64_t) * n, &ce);
+    if (!d_off || !d_N || !d_h || !d_no || !d_po) return fail(EPSCU_ERR_NOMEM, "device arena (adjoint)");
+    cudaStream_t s = ctx->stream;
+    const cudaStream_t caller = caller_stream(opts);
+    EPSCU_CU(cudaEventRecord(ctx->ev_in, caller));
+    EPSCU_CU(cudaStreamWaitEvent(s, ctx->ev_in, 0));
+    EPSCU_CU(cudaMemcpyAsync(d_off, offsets, sizeof(int64_t) * n, cudaMemcpyHostToDevice, s));
+    EPSCU_CU(cudaMemcpyAsync(d_N, N, sizeof(int32_t) * n, cudaMemcpyHostToDevice, s));
+    EPSCU_CU(cudaMemcpyAsync(d_h, h.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    EPSCU_CU(cudaMemcpyAsync(d_no, n_out, sizeof(int32_t) * n, cudaMemcpyHostToDevice, s));
+    EPSCU_CU(cudaMemcpyAsync(d_po, psi_offsets, sizeof(int64_t) * n, cudaMemcpyHostToDevice, s));
+    const double* g_psi = psi;
+    const double* g_E = dL_dE;
+    double* g_V = dL_dV;
+    if (!dev) {
+        auto* a = (double*)ctx->get("adjx_psi", sizeof(double) * std::max<int64_t>(psi_total, 1), &ce);
+        auto* b = (double*)ctx->get("adjx_gE", sizeof(double) * (size_t)n * cap, &ce);
+        auto* c = (double*)ctx->get("adjx_gV", sizeof(double) * std::max<int64_t>(total, 1), &ce);
+        if (!a || !b || !c) return fail(EPSCU_ERR_NOMEM, "device arena (adjoint)");
+        EPSCU_CU(cudaMemcpyAsync(a, psi, sizeof(double) * psi_total, cudaMemcpyHostToDevice, s));
+        EPSCU_CU(cudaMemcpyAsync(b, dL_dE, sizeof(double) * (size_t)n * cap, cudaMemcpyHostToDevice, s));
+        EPSCU_CU(cudaMemsetAsync(c, 0, sizeof(double) * total, s));
+        g_psi = a;
+        g_E = b;
+        g_V = c;
+    }
+    launch_adjoint_explicit(n, cap, max_N, d_off, d_N, d_h, d_no, d_po, g_psi, g_E, g_V, s);
+    EPSCU_CU(cudaGetLastError());
+    if (!dev) EPSCU_CU(cudaMemcpyAsync(dL_dV, g_V, sizeof(double) * total, cudaMemcpyDeviceToHost, s));
+    EPSCU_CU(cudaEventRecord(ctx->ev_out, s));
+    EPSCU_CU(cudaStreamWaitEvent(caller, ctx->ev_out, 0));
+    EPSCU_CU(cudaStreamSynchronize(s));
+    return EPSCU_OK;
+}
+
 extern "C" epscu_status epscu_tabulate(epscu_ctx* ctx, int32_t n, const int32_t* kind, const double* params,
                                        const int64_t* offsets, const int32_t* N, const double* r_min,
                                        const double* r_max, int32_t n_knots, double* V, const epscu_opts* opts_in) {

@@ -70,6 +70,10 @@ void launch_fallback_df(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_adjoint(const DevBatch& b, const double* dL_dE, double* dL_dV, int64_t total_points,
                     const int64_t* offsets_dev, int recompute, int sm_count, cudaStream_t s);
 
+void launch_adjoint_explicit(int32_t n, int32_t cap, int32_t max_N, const int64_t* offsets, const int32_t* N,
+                             const double* h, const int32_t* n_out, const int64_t* psi_off, const double* psi,
+                             const double* gE, double* gV, cudaStream_t s);
+
 // peaks.cu
 void measure_fma_peaks(int sm_count, double* fp32_tflops, double* fp64_tflops);
 

@@ -12,7 +12,7 @@
 //
 //  newton_df : Cooley corrections from the FP32 energy (1..4 passes) inside an
 //              FP64 count bracket; levels that do not settle go to
-//  fallback_df: bisection on compensated-FP32 counts, one level per warp.
+//  fallback_df: multisection on compensated-FP32 counts, one warp per level.
 //  norm_df   : sums, node count, peak of |psi| and the constants of the write.
 //  write_df  : recomputes the pass and writes psi (FP64) to HBM.
 #include <cuda_runtime.h>
@@ -208,38 +208,54 @@ __global__ void __launch_bounds__(kThreads) newton_df_kernel(DevBatch b) {
     }
 }
 
-// Bisection on compensated-FP32 twisted Sturm counts for the levels the Newton
-// stage could not settle (near-degenerate pairs, match points across a
-// barrier).  The FP32 bracket widened by 2e-8 is verified by counts at both
-// ends first; the scan bracket (widened by one trial spacing) is the fallback.
-// One level per warp (lane 0): the list is short and each level is serial.
-__global__ void __launch_bounds__(32) fallback_df_kernel(DevBatch b) {
+// Multisection on compensated-FP32 twisted Sturm counts for the levels the
+// Newton stage could not settle (near-degenerate pairs, match points across a
+// barrier).  One warp per level: lane j counts at lo + (j+1)(hi-lo)/33 and a
+// ballot picks the sub-interval holding the level, so every round gains five
+// bits instead of one.  The FP32 bracket widened by 2e-8 is verified first;
+// the scan bracket widened by one trial spacing is the fallback.
+__global__ void __launch_bounds__(128) fallback_df_kernel(DevBatch b) {
     const int n = min(b.hdr->fallbacks, b.max_levels);
-    if (threadIdx.x != 0) return;
-    for (int q = blockIdx.x; q < n; q += gridDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int n_warps = (gridDim.x * blockDim.x) >> 5;
+    for (int q = warp; q < n; q += n_warps) {
         const int slot = b.fallback_list[q];
         LevelWork w = b.levels[slot];
         const PotMeta m = b.meta[w.p];
         const float2* Wf = b.Wf2 + m.offf;
         const double* W = b.W64 + m.off;
-        auto count_at = [&](double E) { return pass_df<0>(m, Wf, W, E, w.k, 1.0).count; };
         double lo = fmax(m.e_lo, w.lo - 2e-8), hi = fmin(m.e_cap, w.hi + 2e-8);
-        if (!(count_at(lo) <= w.v && count_at(hi) > w.v)) {
-            lo = fmax(m.e_lo, w.lo0 - m.delta);
-            hi = fmin(m.e_cap, w.hi0 + m.delta);
+        {
+            // lane 0 checks lo, lane 1 checks hi
+            const double Ec = lane == 0 ? lo : hi;
+            const int c = lane < 2 ? pass_df<0>(m, Wf, W, Ec, w.k, 1.0).count : 0;
+            const int c_lo = __shfl_sync(0xffffffffu, c, 0), c_hi = __shfl_sync(0xffffffffu, c, 1);
+            if (!(c_lo <= w.v && c_hi > w.v)) {
+                lo = fmax(m.e_lo, w.lo0 - m.delta);
+                hi = fmin(m.e_cap, w.hi0 + m.delta);
+            }
         }
-        for (int it = 0; it < 64; ++it) {
+        for (int round = 0; round < 16; ++round) {
             if (hi - lo <= 1e-12 * fmax(1.0, fabs(lo))) break;
-            const double mid = 0.5 * (lo + hi);
-            if (!(mid > lo && mid < hi)) break;
-            if (count_at(mid) > w.v) hi = mid;
-            else lo = mid;
+            const double step = (hi - lo) / 33.0;
+            const double Ej = lo + (lane + 1) * step;
+            const bool above = pass_df<0>(m, Wf, W, Ej, w.k, 1.0).count > w.v;
+            const unsigned mask = __ballot_sync(0xffffffffu, above);
+            // counts are monotone in E: the first lane above bounds the level
+            const int first = mask ? __ffs(mask) - 1 : 32;
+            const double nlo = first == 0 ? lo : lo + first * step;
+            const double nhi = first == 32 ? hi : lo + (first + 1) * step;
+            lo = nlo;
+            hi = nhi;
         }
-        w.E = 0.5 * (lo + hi);
-        w.lo = lo;
-        w.hi = hi;
-        w.status &= ~EPSCU_STATUS_FALLBACK;
-        b.levels[slot] = w;
+        if (lane == 0) {
+            w.E = 0.5 * (lo + hi);
+            w.lo = lo;
+            w.hi = hi;
+            w.status &= ~EPSCU_STATUS_FALLBACK;
+            b.levels[slot] = w;
+        }
     }
 }
 
@@ -323,7 +339,7 @@ void launch_write_df(const DevBatch& b, int sm_count, cudaStream_t s) {
     write_df_kernel<<<sm_count * 8, kThreads, 0, s>>>(b);
 }
 void launch_fallback_df(const DevBatch& b, int sm_count, cudaStream_t s) {
-    fallback_df_kernel<<<sm_count * 4, 32, 0, s>>>(b);
+    fallback_df_kernel<<<sm_count * 2, 128, 0, s>>>(b);
 }
 
 }  // namespace epscu

@@ -169,6 +169,19 @@ epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, epscu_result*
 epscu_status epscu_adjoint(epscu_ctx* ctx, const double* dL_dE, double* dL_dV, int32_t recompute,
                            const epscu_opts* opts);
 
+/* Stateless form of the adjoint on explicit wavefunctions (as written by
+ * epscu_solve with EPSCU_WANT_PSI):
+ *   dL_dV[offsets[p] + i] = h_p sum_{s < n_out[p]} dL_dE[p*cap + s]
+ *                           * psi[psi_offsets[p] + s N[p] + i]^2,
+ * h_p = (r_max[p] - r_min[p]) / (N[p] - 1).  offsets, N, r_min, r_max, n_out
+ * and psi_offsets are host arrays; psi, dL_dE and dL_dV follow opts->flags
+ * (EPSCU_MEM_DEVICE).  Any number of solves may be differentiated in any
+ * order.  No reference counterpart. */
+epscu_status epscu_adjoint_psi(epscu_ctx* ctx, int32_t n, const int64_t* offsets, const int32_t* N,
+                               const double* r_min, const double* r_max, const int32_t* n_out,
+                               int32_t level_capacity, const double* psi, const int64_t* psi_offsets,
+                               const double* dL_dE, double* dL_dV, const epscu_opts* opts);
+
 /* Tabulate parametric potentials on their grids on the device (Morse, shifted
  * Lennard-Jones, Morse + Gaussian bumps through a natural cubic spline on
  * n_knots uniform knots spanning [r_min, r_max]).  params is [n, 12]: Morse

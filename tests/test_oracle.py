@@ -42,6 +42,11 @@ def test_morse_single_against_dense_and_analytic():
     assert an.size == 14
     # O(h^4) discretisation error of Numerov on this grid
     assert np.max(np.abs(s.energy_polished - an)) < 5e-9
+    # dense eigen-decomposition of the same discretisation on a coarser grid
+    b = synth.morse_single(N=1400)
+    V = b.V(0)
+    s = O.solve_batch([V], b.r_min, b.r_max, b.mu, b.e_cap, b.n_trial, want_psi=True)[0]
+    assert s.n_total == 14
     w, U = dense_levels(V, s.grid, b.mu[0], 14)
     assert np.max(np.abs(s.energy_polished - w)) < 1e-12
     assert np.max(np.abs(s.energy - w)) < 1e-12  # bisection to 1e-12
@@ -107,7 +112,7 @@ def test_hellmann_feynman_matches_fd():
 def test_double_well_inner_level_wavefunction():
     # Morse with a tall Gaussian barrier: a double well whose inner levels are
     # invisible at the outer turning point; the match point must move.
-    r = np.linspace(0.5, 12.0, 3000)
+    r = np.linspace(0.5, 12.0, 1500)
     V = synth.morse(r, 0.1, 1.0, 2.0) + synth.bumps_at(r, [(0.08, 0.25, 2.6)])
     s = O.solve_batch([V], 0.5, 12.0, 2000.0, 0.0999, 512, want_psi=True)[0]
     g = s.grid
