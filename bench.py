@@ -211,6 +211,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--batch", type=int, default=2048,
+                    help="potentials per GPU (2048 = the measured workload; smaller for profiler captures)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
@@ -234,7 +236,7 @@ def main():
 
     ctx = capi.Context(local)
     fp32_peak, fp64_peak = ctx.measure_fma_peaks()
-    b = workload(rank)
+    b = workload(rank, B=args.batch)
     Vs = b.potentials()
     cap = 512
 

@@ -65,11 +65,18 @@ struct Header {
     int32_t queue_polish;
     int32_t error;          // first device-side error code (0 = none)
     int32_t fallbacks;      // levels that needed the bisection fallback
-    int32_t pad[2];
+    int32_t n_units;        // warp work units (<= 32 levels of one potential)
+    int32_t n_twist;        // levels handed to the twist-index search
+    int32_t queue[8];       // work-queue heads of the per-level kernels
 };
+
+// queue ids of the per-level kernels
+enum { kQRefine32 = 0, kQNewtonDF, kQNormDF, kQWriteDF, kQBisect64, kQNorm64, kQWrite64 };
 
 // internal level flag: the Newton stage handed the level to the bisection fallback
 #define EPSCU_STATUS_FALLBACK 0x10000
+// spacing of the samples of the twist-index search
+constexpr int kTwistSample = 64;
 
 // ---------------------------------------------------------------- FP64 helpers
 

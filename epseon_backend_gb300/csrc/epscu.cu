@@ -292,6 +292,7 @@ void enqueue_pipeline(epscu_ctx* ctx, const DevBatch& b, int method, bool want_p
         launch_bisect64(b, ctx->sm_count, s);
         rec(3);
         launch_norm64(b, 0, ctx->sm_count, s);
+        launch_twist64(b, ctx->sm_count, s);
         rec(4);
         if (want_psi) launch_write64(b, ctx->sm_count, s);
     } else {
@@ -300,6 +301,7 @@ void enqueue_pipeline(epscu_ctx* ctx, const DevBatch& b, int method, bool want_p
         launch_newton_df(b, ctx->sm_count, s);
         launch_fallback_df(b, ctx->sm_count, s);
         launch_norm_df(b, ctx->sm_count, s);
+        launch_twist_df(b, ctx->sm_count, s);
         rec(4);
         if (want_psi) launch_write_df(b, ctx->sm_count, s);
     }
@@ -393,10 +395,15 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     b.counts = (int32_t*)ctx->get("counts", sizeof(int32_t) * (size_t)n * batch->n_trial, &ce);
     b.levels = (LevelWork*)ctx->get("levels", sizeof(LevelWork) * lv, &ce);
     b.fallback_list = (int32_t*)ctx->get("fallback_list", sizeof(int32_t) * lv, &ce);
+    b.max_units = (int32_t)(n + lv / 32 + 1);
+    b.units = (int2*)ctx->get("units", sizeof(int2) * (size_t)b.max_units, &ce);
+    b.max_twist = 4096;
+    b.twist_list = (int32_t*)ctx->get("twist_list", sizeof(int32_t) * b.max_twist, &ce);
     b.hdr = (Header*)ctx->get("hdr", sizeof(Header), &ce);
     b.order = (int32_t*)ctx->get("order", sizeof(int32_t) * n, &ce);
     int64_t* d_off = (int64_t*)ctx->get("offsets", sizeof(int64_t) * n, &ce);
-    if (ce != cudaSuccess || !b.meta || !b.W64 || !b.Msuf || !b.counts || !b.levels || !b.fallback_list || !b.hdr ||
+    if (ce != cudaSuccess || !b.meta || !b.W64 || !b.Msuf || !b.counts || !b.levels || !b.fallback_list || !b.units ||
+        !b.hdr ||
         !b.order || !d_off ||
         (method == EPSCU_METHOD_FAST_FP32C && !b.Wf2))
         return fail(EPSCU_ERR_NOMEM, std::string("device arena: ") + cudaGetErrorString(ce));
@@ -414,6 +421,9 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     b.min_level = batch->min_level;
     b.max_level = batch->max_level;
     b.max_N = max_N;
+    b.twist_stride = max_N / kTwistSample + 4;
+    b.twist_scratch = (double*)ctx->get("twist_scratch", sizeof(double) * (size_t)b.max_twist * b.twist_stride, &ce);
+    if (!b.twist_scratch || !b.twist_list) return fail(EPSCU_ERR_NOMEM, "device arena (twist search)");
     b.tol = opts.tol;
     b.psi = nullptr;
     b.psi_capacity = 0;
@@ -601,7 +611,7 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     st.n_levels = nlev;
     st.fallbacks = hh->fallbacks;
     st.psi_bytes = want_psi ? psi_total * 8 : 0;
-    st.kernel_launches = 7 + (want_psi ? 1 : 0) + (method == EPSCU_METHOD_FAST_FP32C ? 2 : 0);
+    st.kernel_launches = 9 + (want_psi ? 1 : 0) + (method == EPSCU_METHOD_FAST_FP32C ? 2 : 0);
     if (method == EPSCU_METHOD_PLAIN_FP64) {
         st.refine_point_updates = 0;
         int64_t bis = 0;
@@ -650,7 +660,11 @@ extern "C" epscu_status epscu_adjoint(epscu_ctx* ctx, const double* dL_dE, doubl
         if (!psi) return fail(EPSCU_ERR_NOMEM, "device arena (recomputed psi)");
         b.psi = psi;
         b.psi_capacity = ctx->last_psi_total;
-        launch_write64(b, ctx->sm_count, s);
+        // the writer of the solve's own method (its norm constants belong to it)
+        const int qid = ctx->last_method == EPSCU_METHOD_FAST_FP32C ? kQWriteDF : kQWrite64;
+        EPSCU_CU(cudaMemsetAsync(&b.hdr->queue[qid], 0, sizeof(int32_t), s));
+        if (ctx->last_method == EPSCU_METHOD_FAST_FP32C) launch_write_df(b, ctx->sm_count, s);
+        else launch_write64(b, ctx->sm_count, s);
     }
     const bool dev = (opts.flags & EPSCU_MEM_DEVICE) != 0;
     const int64_t lv = (int64_t)b.n * b.level_capacity;

@@ -19,6 +19,11 @@ struct DevBatch {
     int32_t* counts;           // [n * n_trial]
     LevelWork* levels;         // [max_levels]
     int32_t* fallback_list;    // [max_levels] slots handed to the bisection fallback
+    int2* units;               // [max_units] (first slot, count) per warp work unit
+    int32_t max_units;
+    int32_t* twist_list;       // [max_twist] slots for the twist-index search
+    double* twist_scratch;     // [max_twist * twist_stride] sampled outward ratios
+    int32_t max_twist, twist_stride;
     int32_t max_levels;        // capacity of levels (n * level_capacity)
     int32_t level_capacity;    // slots per potential
     Header* hdr;
@@ -31,6 +36,18 @@ struct DevBatch {
     int32_t max_N;             // longest grid of the batch
     double tol;
 };
+
+// Warp-level work queue of the per-level kernels: units of up to 32
+// consecutive level slots of one potential, longest grids first.  Lane 0
+// takes the next unit and broadcasts it; false when the queue is drained.
+__device__ __forceinline__ bool next_unit(const DevBatch& b, int qid, int2& unit) {
+    int u = 0;
+    if ((threadIdx.x & 31) == 0) u = atomicAdd(&b.hdr->queue[qid], 1);
+    u = __shfl_sync(0xffffffffu, u, 0);
+    if (u >= b.hdr->n_units || u >= b.max_units) return false;
+    unit = b.units[u];
+    return true;
+}
 
 // prepare.cu
 void launch_prepare(const DevBatch& b, cudaStream_t s);
@@ -65,6 +82,8 @@ void launch_newton_df(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_norm_df(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_write_df(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_fallback_df(const DevBatch& b, int sm_count, cudaStream_t s);
+void launch_twist_df(const DevBatch& b, int sm_count, cudaStream_t s);
+void launch_twist64(const DevBatch& b, int sm_count, cudaStream_t s);
 
 // adjoint.cu
 void launch_adjoint(const DevBatch& b, const double* dL_dE, double* dL_dV, int64_t total_points,

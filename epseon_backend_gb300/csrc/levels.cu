@@ -186,8 +186,9 @@ __device__ __forceinline__ double gamma64(const PotMeta& m, const double* __rest
 // ----------------------------------------------------------------- kernels
 
 __global__ void __launch_bounds__(kLevelThreads) bisect64_kernel(DevBatch b) {
-    const int total = b.hdr->total_levels;
-    for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < total; slot += gridDim.x * blockDim.x) {
+    for (int2 unit; next_unit(b, kQBisect64, unit);) {
+        if ((int)(threadIdx.x & 31) >= unit.y) continue;
+        const int slot = unit.x + (threadIdx.x & 31);
         LevelWork w = b.levels[slot];
         if (w.status & EPSCU_STATUS_NOTFOUND) continue;
         if (cancelled(b)) {
@@ -234,11 +235,13 @@ __device__ __forceinline__ Pass32 cooley32(const PotMeta& m, const float2* __res
         const int dir = side == 0 ? 1 : -1;
         int ecum = 0;
         const int nsteps = (to - from) * dir;
-        // 8 loads in flight per thread: the grid values do not depend on the state
-        for (int base = 0; base < nsteps; base += 8) {
-            float2 w8[8];
+        // grid values do not depend on the state: two 8-point chunks in flight
+        // (register double buffer) hide the load latency behind the recurrence
+        auto load8 = [&](float2* w8, int base) {
 #pragma unroll
             for (int u = 0; u < 8; ++u) w8[u] = __ldg(Wf + from + dir * min(base + u, nsteps - 1));
+        };
+        auto run8 = [&](const float2* w8, int base) {
 #pragma unroll
             for (int u = 0; u < 8; ++u) {
                 if (base + u < nsteps) {
@@ -254,22 +257,29 @@ __device__ __forceinline__ Pass32 cooley32(const PotMeta& m, const float2* __res
                 }
             }
             const int i = from + dir * min(base + 7, nsteps - 1);
-            {
-                const float mm = fmaxf(fabsf(A), fabsf(D));
-                const int e = ((__float_as_int(mm) >> 23) & 0xff) - 126;
-                if (mm > 0.0f && e > -60 && e < 60) {
-                    const float sc = __int_as_float((127 - e) << 23);
-                    A *= sc;
-                    D *= sc;
-                    S *= sc * sc;
-                    ecum += e;
-                }
-                const int L = ecum + ((__float_as_int(fabsf(A)) >> 23) & 0xff);
-                if (A != 0.0f && L > Lpk[side]) {
-                    Lpk[side] = L;
-                    ipk[side] = i;
-                }
+            const float mm = fmaxf(fabsf(A), fabsf(D));
+            const int e = ((__float_as_int(mm) >> 23) & 0xff) - 126;
+            if (mm > 0.0f && e > -60 && e < 60) {
+                const float sc = __int_as_float((127 - e) << 23);
+                A *= sc;
+                D *= sc;
+                S *= sc * sc;
+                ecum += e;
             }
+            const int L = ecum + ((__float_as_int(fabsf(A)) >> 23) & 0xff);
+            if (A != 0.0f && L > Lpk[side]) {
+                Lpk[side] = L;
+                ipk[side] = i;
+            }
+        };
+        float2 wa[8], wb[8];
+        if (nsteps > 0) load8(wa, 0);
+        for (int base = 0; base < nsteps; base += 16) {
+            if (base + 8 < nsteps) load8(wb, base + 8);
+            run8(wa, base);
+            if (base + 8 >= nsteps) break;
+            if (base + 16 < nsteps) load8(wa, base + 16);
+            run8(wb, base + 8);
         }
         Lk[side] = ecum + (A != 0.0f ? ((__float_as_int(fabsf(A)) >> 23) & 0xff) : -1000);
         if (side == 0) {
@@ -308,8 +318,9 @@ __device__ __forceinline__ Pass32 cooley32(const PotMeta& m, const float2* __res
 constexpr double kTol32 = 2e-9;
 
 __global__ void __launch_bounds__(kLevelThreads) refine32_kernel(DevBatch b) {
-    const int total = b.hdr->total_levels;
-    for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < total; slot += gridDim.x * blockDim.x) {
+    for (int2 unit; next_unit(b, kQRefine32, unit);) {
+        if ((int)(threadIdx.x & 31) >= unit.y) continue;
+        const int slot = unit.x + (threadIdx.x & 31);
         LevelWork w = b.levels[slot];
         if (w.status & EPSCU_STATUS_NOTFOUND) continue;
         if (cancelled(b)) {
@@ -421,12 +432,30 @@ __global__ void __launch_bounds__(kLevelThreads) newton64_kernel(DevBatch b) {
     }
 }
 
+// Write the normalisation constants of pass r (match point k) into w.
+__device__ __forceinline__ void finalize64(const PotMeta& m, LevelWork& w, const Pass64& r, int k) {
+    double ck = 1.0 / sqrt(m.h * r.sum);
+    if (r.pk_out < 0.0) ck = -ck;  // psi > 0 next to the inner wall
+    w.k = k;
+    w.ck = ck;
+    w.norm_k_out = ck / r.pk_out;
+    w.norm_k_in = ck / r.pk_in;
+    w.ex_out = r.ex_out;
+    w.ex_in = r.ex_in;
+    w.dE = r.dE;
+    w.nodes = r.nodes;
+    w.status &= ~EPSCU_STATUS_NOTFOUND;
+    if (!isfinite(r.dE) || !isfinite(ck)) w.status |= EPSCU_STATUS_NONFINITE;
+    if (r.nodes != w.v && !(m.status & EPSCU_STATUS_UNDER)) w.status |= EPSCU_STATUS_NOTFOUND;
+}
+
 // use_k: keep the match point chosen by the FP32 refinement (fast method);
 // otherwise the outer turning point, moved to the peak of |psi| of the solution
 // stitched there (as the oracle's match point).
 __global__ void __launch_bounds__(kLevelThreads) norm64_kernel(DevBatch b, int use_k) {
-    const int total = b.hdr->total_levels;
-    for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < total; slot += gridDim.x * blockDim.x) {
+    for (int2 unit; next_unit(b, kQNorm64, unit);) {
+        if ((int)(threadIdx.x & 31) >= unit.y) continue;
+        const int slot = unit.x + (threadIdx.x & 31);
         LevelWork w = b.levels[slot];
         if (w.status & (EPSCU_STATUS_NOTFOUND | EPSCU_STATUS_CANCELLED)) continue;
         const PotMeta m = b.meta[w.p];
@@ -436,26 +465,74 @@ __global__ void __launch_bounds__(kLevelThreads) norm64_kernel(DevBatch b, int u
             k = clamp_inner(m, r.peak_i);
             r = cooley64<true>(m, b.W64 + m.off, w.E, k);
         }
-        double ck = 1.0 / sqrt(m.h * r.sum);
-        if (r.pk_out < 0.0) ck = -ck;  // psi > 0 next to the inner wall
-        w.k = k;
-        w.ck = ck;
-        w.norm_k_out = ck / r.pk_out;
-        w.norm_k_in = ck / r.pk_in;
-        w.ex_out = r.ex_out;
-        w.ex_in = r.ex_in;
-        w.dE = r.dE;
-        w.nodes = r.nodes;
-        if (!isfinite(r.dE) || !isfinite(ck)) w.status |= EPSCU_STATUS_NONFINITE;
-        if (r.nodes != w.v) w.status |= EPSCU_STATUS_NOTFOUND;
+        finalize64(m, w, r, k);
+        // a poor match point shows as a wrong node count or as a Cooley
+        // correction far above the accuracy of the bisected energy
+        const bool bad = (r.nodes != w.v && !(m.status & EPSCU_STATUS_UNDER)) ||
+                         !(fabs(r.dE) <= 1e-11 * fmax(1.0, fabs(w.E)));
+        if (bad && b.twist_list) {
+            const int q = atomicAdd(&b.hdr->n_twist, 1);
+            if (q < b.max_twist) b.twist_list[q] = slot;
+        }
+        b.levels[slot] = w;
+    }
+}
+
+// Twist-index search of the plain method (FP64): sampled outward ratios
+// u_{k-1}/u_k, inward ratios v_{k+1}/v_k, match point argmin |gamma_k|.
+__global__ void __launch_bounds__(64) twist64_kernel(DevBatch b) {
+    const int n = min(b.hdr->n_twist, b.max_twist);
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const int slot = b.twist_list[q];
+        LevelWork w = b.levels[slot];
+        const PotMeta m = b.meta[w.p];
+        const double* W = b.W64 + m.off;
+        double* rho = b.twist_scratch + (int64_t)q * b.twist_stride;
+        const double aE = __dmul_rn(m.a, w.E);
+        double A = 1.0, B = 0.0;
+        int s = 0;
+        for (int i = m.i0; i < m.i1; ++i) {
+            const int j = (i - m.i0) / kTwistSample;
+            if ((i - m.i0) % kTwistSample == 0 && j < b.twist_stride) rho[j] = B / A;
+            step64(aE, __ldg(W + i), A, B);
+            if (++s == kRenorm) {
+                s = 0;
+                renorm_pair(A, B);
+            }
+        }
+        double C = 1.0, D = 0.0, best = INFINITY;
+        int kbest = w.k;
+        s = 0;
+        for (int i = m.i1; i > m.i0; --i) {
+            if ((i - m.i0) % kTwistSample == 0 && i <= m.i1 - 1) {
+                const int j = (i - m.i0) / kTwistSample;
+                if (j < b.twist_stride) {
+                    const double T = __dsub_rn(aE, __ldg(W + i));
+                    const double gam = (2.0 - 10.0 * T) / (1.0 + T) - rho[j] - D / C;
+                    if (fabs(gam) < best) {
+                        best = fabs(gam);
+                        kbest = i;
+                    }
+                }
+            }
+            step64(aE, __ldg(W + i), C, D);
+            if (++s == kRenorm) {
+                s = 0;
+                renorm_pair(C, D);
+            }
+        }
+        const int k = clamp_inner(m, kbest);
+        const Pass64 r = cooley64<true>(m, W, w.E, k);
+        finalize64(m, w, r, k);
         b.levels[slot] = w;
     }
 }
 
 __global__ void __launch_bounds__(kLevelThreads) write64_kernel(DevBatch b) {
-    const int total = b.hdr->total_levels;
     if (!b.psi || b.hdr->error) return;
-    for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < total; slot += gridDim.x * blockDim.x) {
+    for (int2 unit; next_unit(b, kQWrite64, unit);) {
+        if ((int)(threadIdx.x & 31) >= unit.y) continue;
+        const int slot = unit.x + (threadIdx.x & 31);
         const LevelWork w = b.levels[slot];
         const PotMeta m = b.meta[w.p];
         double* out = b.psi + m.psi_off + (int64_t)(w.v - b.min_level) * m.N;
@@ -514,6 +591,9 @@ void launch_newton64(const DevBatch& b, int sm_count, cudaStream_t s) {
 }
 void launch_norm64(const DevBatch& b, int use_k, int sm_count, cudaStream_t s) {
     norm64_kernel<<<persistent_grid(sm_count, 8), kLevelThreads, 0, s>>>(b, use_k);
+}
+void launch_twist64(const DevBatch& b, int sm_count, cudaStream_t s) {
+    twist64_kernel<<<sm_count, 64, 0, s>>>(b);
 }
 void launch_write64(const DevBatch& b, int sm_count, cudaStream_t s) {
     write64_kernel<<<persistent_grid(sm_count, 8), kLevelThreads, 0, s>>>(b);

@@ -56,10 +56,12 @@ __device__ __forceinline__ void side_df(const float2* __restrict__ Wf, dfl aE, i
     dfl F = {0.0f, 0.0f};
     if (MODE == 2) F = df_from_double(L * ldexp(1.0, min(1000, max(-1100, -Xk))));
     const int nsteps = (to - from) * dir;
-    for (int base = 0; base < nsteps; base += 8) {
-        float2 w8[8];  // 8 grid values in flight: they do not depend on the state
+    // two 8-point chunks of grid values in flight (register double buffer)
+    auto load8 = [&](float2* w8, int base) {
 #pragma unroll
         for (int u = 0; u < 8; ++u) w8[u] = __ldg(Wf + from + dir * min(base + u, nsteps - 1));
+    };
+    auto run8 = [&](const float2* w8, int base) {
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
             if (base + u >= nsteps) break;
@@ -118,6 +120,15 @@ __device__ __forceinline__ void side_df(const float2* __restrict__ Wf, dfl aE, i
                 F = df_from_double(L * ldexp(1.0, min(1000, max(-1100, st.eA + st.eQ - Xk))));
             }
         }
+        };
+    float2 wa[8], wb[8];
+    if (nsteps > 0) load8(wa, 0);
+    for (int base = 0; base < nsteps; base += 16) {
+        if (base + 8 < nsteps) load8(wb, base + 8);
+        run8(wa, base);
+        if (base + 8 >= nsteps) break;
+        if (base + 16 < nsteps) load8(wa, base + 16);
+        run8(wb, base + 8);
     }
     if (MODE == 1) st.S += f2d(Sacc.h) + f2d(Sacc.l);
 }
@@ -176,8 +187,9 @@ __device__ PassDF pass_df(const PotMeta& m, const float2* __restrict__ Wf, const
 }
 
 __global__ void __launch_bounds__(kThreads) newton_df_kernel(DevBatch b) {
-    const int total = b.hdr->total_levels;
-    for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < total; slot += gridDim.x * blockDim.x) {
+    for (int2 unit; next_unit(b, kQNewtonDF, unit);) {
+        if ((int)(threadIdx.x & 31) >= unit.y) continue;
+        const int slot = unit.x + (threadIdx.x & 31);
         LevelWork w = b.levels[slot];
         if (w.status & (EPSCU_STATUS_NOTFOUND | EPSCU_STATUS_CANCELLED)) continue;
         const PotMeta m = b.meta[w.p];
@@ -259,9 +271,33 @@ __global__ void __launch_bounds__(128) fallback_df_kernel(DevBatch b) {
     }
 }
 
+// Write the normalisation constants of pass r (match point k) into w.
+__device__ __forceinline__ void finalize_df(const PotMeta& m, LevelWork& w, const PassDF& r, int k) {
+    double ck = 1.0 / sqrt(m.h * r.sum);
+    if (r.pk_out < 0.0) ck = -ck;  // psi > 0 next to the inner wall
+    w.k = k;
+    w.ck = ck;
+    w.norm_k_out = ck / r.pk_out;
+    w.norm_k_in = ck / r.pk_in;
+    w.ex_out = r.ex_out;
+    w.ex_in = r.ex_in;
+    w.dE = r.dE;
+    w.nodes = r.nodes;
+    w.status &= ~EPSCU_STATUS_NOTFOUND;
+    if (!isfinite(r.dE) || !isfinite(ck)) w.status |= EPSCU_STATUS_NONFINITE;
+    if (r.nodes != w.v && !(m.status & EPSCU_STATUS_UNDER)) w.status |= EPSCU_STATUS_NOTFOUND;
+}
+
+// a converged level whose final pass disagrees (node count, or a Cooley
+// correction far above the energy's accuracy) was matched at a poor point
+__device__ __forceinline__ bool suspicious(const PotMeta& m, const LevelWork& w, int nodes, double dE) {
+    return (nodes != w.v && !(m.status & EPSCU_STATUS_UNDER)) || !(fabs(dE) <= 1e-11 * fmax(1.0, fabs(w.E)));
+}
+
 __global__ void __launch_bounds__(kThreads) norm_df_kernel(DevBatch b) {
-    const int total = b.hdr->total_levels;
-    for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < total; slot += gridDim.x * blockDim.x) {
+    for (int2 unit; next_unit(b, kQNormDF, unit);) {
+        if ((int)(threadIdx.x & 31) >= unit.y) continue;
+        const int slot = unit.x + (threadIdx.x & 31);
         LevelWork w = b.levels[slot];
         if (w.status & (EPSCU_STATUS_NOTFOUND | EPSCU_STATUS_CANCELLED)) continue;
         const PotMeta m = b.meta[w.p];
@@ -289,26 +325,95 @@ __global__ void __launch_bounds__(kThreads) norm_df_kernel(DevBatch b) {
                 k = k2;
             }
         }
-        double ck = 1.0 / sqrt(m.h * r.sum);
-        if (r.pk_out < 0.0) ck = -ck;  // psi > 0 next to the inner wall
-        w.k = k;
-        w.ck = ck;
-        w.norm_k_out = ck / r.pk_out;
-        w.norm_k_in = ck / r.pk_in;
-        w.ex_out = r.ex_out;
-        w.ex_in = r.ex_in;
-        w.dE = r.dE;
-        w.nodes = r.nodes;
-        if (!isfinite(r.dE) || !isfinite(ck)) w.status |= EPSCU_STATUS_NONFINITE;
-        if (r.nodes != w.v && !(m.status & EPSCU_STATUS_UNDER)) w.status |= EPSCU_STATUS_NOTFOUND;
+        finalize_df(m, w, r, k);
+        if (suspicious(m, w, r.nodes, r.dE) && b.twist_list) {
+            const int q = atomicAdd(&b.hdr->n_twist, 1);
+            if (q < b.max_twist) b.twist_list[q] = slot;
+        }
+        b.levels[slot] = w;
+    }
+}
+
+// Twist-index search for the levels norm_df flagged: one full outward sweep
+// samples u_{k-1}/u_k every kTwistSample points, one full inward sweep forms
+// gamma_k at the same points, and the match point becomes argmin |gamma_k|
+// (at an eigenvalue |gamma_k| is smallest where the eigenvector is largest;
+// the rule of Dhillon and Parlett's twisted factorisations).  Then the norm
+// pass is redone there.
+__global__ void __launch_bounds__(64) twist_df_kernel(DevBatch b) {
+    const int n = min(b.hdr->n_twist, b.max_twist);
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const int slot = b.twist_list[q];
+        LevelWork w = b.levels[slot];
+        const PotMeta m = b.meta[w.p];
+        const float2* Wf = b.Wf2 + m.offf;
+        const double* W = b.W64 + m.off;
+        double* rho = b.twist_scratch + (int64_t)q * b.twist_stride;
+        const dfl aE = energy_df(m, w.E);
+        const double aEd = __dmul_rn(m.a, w.E);
+        // outward: before point i the state is ~ (u_i, u_i - u_{i-1})
+        dfl A = {1.0f, 0.0f}, D = {1.0f, 0.0f};
+        for (int i = m.i0; i < m.i1; ++i) {
+            const int j = (i - m.i0) / kTwistSample;
+            if ((i - m.i0) % kTwistSample == 0 && j < b.twist_stride) rho[j] = df_to_double(D) / df_to_double(A);
+            const float2 wv = __ldg(Wf + i);
+            dfl T = two_sum(aE.h, -wv.x);
+            T = fast_two_sum(T.h, __fadd_rn(T.l, __fsub_rn(aE.l, wv.y)));
+            const dfl X = df_add(D, df_mulf(A, -12.0f));
+            D = df_add(D, df_mul(T, X));
+            A = df_add(A, df_add(df_mul(T, A), D));
+            if (((i - m.i0) & 7) == 7) {
+                const float mm = fmaxf(fabsf(A.h), fabsf(D.h));
+                if (mm > 0.0f && mm < INFINITY) {
+                    const float sc = fpow2(-max(-120, min(120, fexp(mm))));
+                    A = df_scale(A, sc);
+                    D = df_scale(D, sc);
+                }
+            }
+        }
+        // inward: before point i the state is ~ (v_i, v_i - v_{i+1})
+        dfl C = {1.0f, 0.0f}, E = {1.0f, 0.0f};
+        double best = INFINITY;
+        int kbest = w.k;
+        for (int i = m.i1; i > m.i0; --i) {
+            if ((i - m.i0) % kTwistSample == 0 && i <= m.i1 - 1) {
+                const int j = (i - m.i0) / kTwistSample;
+                if (j < b.twist_stride) {
+                    const double Ti = aEd - __ldg(W + i);
+                    const double gam = -12.0 * Ti / (1.0 + Ti) + rho[j] + df_to_double(E) / df_to_double(C);
+                    if (fabs(gam) < best) {
+                        best = fabs(gam);
+                        kbest = i;
+                    }
+                }
+            }
+            const float2 wv = __ldg(Wf + i);
+            dfl T = two_sum(aE.h, -wv.x);
+            T = fast_two_sum(T.h, __fadd_rn(T.l, __fsub_rn(aE.l, wv.y)));
+            const dfl X = df_add(E, df_mulf(C, -12.0f));
+            E = df_add(E, df_mul(T, X));
+            C = df_add(C, df_add(df_mul(T, C), E));
+            if (((m.i1 - i) & 7) == 7) {
+                const float mm = fmaxf(fabsf(C.h), fabsf(E.h));
+                if (mm > 0.0f && mm < INFINITY) {
+                    const float sc = fpow2(-max(-120, min(120, fexp(mm))));
+                    C = df_scale(C, sc);
+                    E = df_scale(E, sc);
+                }
+            }
+        }
+        const int k = clamp_k(m, kbest);
+        const PassDF r = pass_df<1>(m, Wf, W, w.E, k, 1.0);
+        finalize_df(m, w, r, k);
         b.levels[slot] = w;
     }
 }
 
 __global__ void __launch_bounds__(kThreads) write_df_kernel(DevBatch b) {
-    const int total = b.hdr->total_levels;
     if (!b.psi || b.hdr->error) return;
-    for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < total; slot += gridDim.x * blockDim.x) {
+    for (int2 unit; next_unit(b, kQWriteDF, unit);) {
+        if ((int)(threadIdx.x & 31) >= unit.y) continue;
+        const int slot = unit.x + (threadIdx.x & 31);
         const LevelWork w = b.levels[slot];
         const PotMeta m = b.meta[w.p];
         double* out = b.psi + m.psi_off + (int64_t)(w.v - b.min_level) * m.N;
@@ -337,6 +442,9 @@ void launch_norm_df(const DevBatch& b, int sm_count, cudaStream_t s) {
 }
 void launch_write_df(const DevBatch& b, int sm_count, cudaStream_t s) {
     write_df_kernel<<<sm_count * 8, kThreads, 0, s>>>(b);
+}
+void launch_twist_df(const DevBatch& b, int sm_count, cudaStream_t s) {
+    twist_df_kernel<<<sm_count, 64, 0, s>>>(b);
 }
 void launch_fallback_df(const DevBatch& b, int sm_count, cudaStream_t s) {
     fallback_df_kernel<<<sm_count * 2, 128, 0, s>>>(b);

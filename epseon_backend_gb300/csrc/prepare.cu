@@ -215,6 +215,45 @@ __global__ void __launch_bounds__(1024) level_setup_kernel(DevBatch b) {
     }
 }
 
+// Warp work units for the per-level kernels: each potential's level slots in
+// chunks of 32, potentials in decreasing grid length (the `order` array), so
+// the warp queue hands out the longest work first.  One CTA.
+__global__ void __launch_bounds__(1024) unit_setup_kernel(DevBatch b) {
+    __shared__ int32_t s_u[1024];
+    __shared__ int32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < b.n; base += blockDim.x) {
+        const int q = base + threadIdx.x;
+        int32_t nu = 0;
+        int p = 0;
+        if (q < b.n) {
+            p = b.order[q];
+            nu = (b.meta[p].n_out + 31) / 32;
+        }
+        s_u[threadIdx.x] = nu;
+        __syncthreads();
+        for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+            const int32_t x = threadIdx.x >= o ? s_u[threadIdx.x - o] : 0;
+            __syncthreads();
+            s_u[threadIdx.x] += x;
+            __syncthreads();
+        }
+        if (q < b.n) {
+            const int32_t first = carry + s_u[threadIdx.x] - nu;
+            const PotMeta& m = b.meta[p];
+            for (int u = 0; u < nu; ++u) {
+                const int32_t at = first + u;
+                if (at < b.max_units) b.units[at] = make_int2(m.level_base + 32 * u, min(32, m.n_out - 32 * u));
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry += s_u[threadIdx.x];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) b.hdr->n_units = min(carry, b.max_units);
+}
+
 // Bracket of every level slot from the scan counts: first trial j with
 // count_j > v; bracket [E_{j-1}, E_j] (E_{-1} = E_lo).
 __global__ void bracket_kernel(DevBatch b) {
@@ -335,6 +374,7 @@ void launch_prepare(const DevBatch& b, cudaStream_t s) {
 
 void launch_level_setup(const DevBatch& b, cudaStream_t s) {
     level_setup_kernel<<<1, 1024, 0, s>>>(b);
+    unit_setup_kernel<<<1, 1024, 0, s>>>(b);
     bracket_kernel<<<b.n, 128, 0, s>>>(b);
 }
 

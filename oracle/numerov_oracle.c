@@ -235,17 +235,38 @@ static int32_t clamp_inner(const eo_grid* g, int32_t k) {
     return k;
 }
 
-/* Match point: the peak of |psi| of the solution stitched at the outer
- * classical turning point, kept off the two boundary points.  Matching where
- * the eigenvector is largest keeps Cooley's correction in its quadratic regime
- * (at a turning point where psi is small -- inner-well levels of a double
- * well, turning points beyond a cut-off grid -- it is not). */
+/* Match point: the twist index k minimising |gamma_k(E)| over i0+1..i1-1,
+ * gamma_k = c_k - u_{k-1}/u_k - v_{k+1}/v_k from one full outward and one full
+ * inward sweep (the twisted-factorisation rule of Dhillon and Parlett's MRRR:
+ * at an eigenvalue |gamma_k| is smallest where the eigenvector is largest).
+ * Matching there keeps Cooley's correction quadratic and the stitched vector
+ * accurate, also for levels separated from the turning point by a barrier. */
 int32_t eo_match_point(const double* V, const eo_grid* g, double E) {
-    const int32_t k = clamp_inner(g, eo_match_index(V, g, E));
-    double* tmp = (double*)malloc(sizeof(double) * (size_t)g->N);
-    const int32_t m = wavefunction_k(V, g, E, k, tmp, NULL);
-    free(tmp);
-    return clamp_inner(g, m);
+    const double a = g->a, aE = a * E;
+    double* rho = (double*)malloc(sizeof(double) * (size_t)g->N);
+    double A = 1.0, B = 0.0;
+    int32_t s = 0;
+    for (int32_t i = g->i0; i < g->i1; ++i) {
+        rho[i] = B / A; /* u_{i-1} / u_i */
+        numerov_step(aE, a * V[i], &A, &B);
+        if (++s == RENORM) { s = 0; renorm2(&A, &B, NULL); }
+    }
+    rho[g->i1] = B / A;
+    double C = 1.0, D = 0.0, best = INFINITY;
+    int32_t kbest = clamp_inner(g, eo_match_index(V, g, E));
+    s = 0;
+    for (int32_t i = g->i1; i > g->i0; --i) {
+        /* here (C, D) ~ (v_i, v_{i+1}) */
+        if (i <= g->i1 - 1) {
+            const double Ti = aE - a * V[i];
+            const double gam = fabs((2.0 - 10.0 * Ti) / (1.0 + Ti) - rho[i] - D / C);
+            if (gam < best) { best = gam; kbest = i; }
+        }
+        numerov_step(aE, a * V[i], &C, &D);
+        if (++s == RENORM) { s = 0; renorm2(&C, &D, NULL); }
+    }
+    free(rho);
+    return clamp_inner(g, kbest);
 }
 
 void eo_wavefunction(const double* V, const eo_grid* g, double E, double* psi) {

@@ -130,3 +130,25 @@ def test_adjoint_matches_finite_differences(ctx):
         rm = O.solve_batch([Vm], b.r_min, b.r_max, b.mu, b.e_cap, b.n_trial)[0]
         fd = np.sum(w * (rp.energy_polished - rm.energy_polished)) / (2 * hfd)
         assert abs(gV[i] - fd) <= 1e-6 * max(abs(fd), 1e-3)
+
+
+@pytest.mark.parametrize("method", [capi.METHOD_PLAIN_FP64, capi.METHOD_FAST_FP32C])
+def test_adjoint_recompute_equals_stored(ctx, method):
+    """The adjoint with psi recomputed (nothing stored by the solve) equals the
+    adjoint on the stored wavefunctions, for both methods."""
+    b = synth.mixed_batch(B=9, n_min=2048, n_max=6000)
+    b.n_trial = 2048
+    Vs = b.potentials()
+    cap = 256
+    s1 = ctx.solve(Vs, b.r_min, b.r_max, b.mu, b.e_cap, b.n_trial, method=method, want_psi=True, level_capacity=cap)
+    rng = np.random.default_rng(5)
+    gE = rng.uniform(0.5, 1.0, (len(b), cap)) * (np.arange(cap)[None, :] < s1.n_out[:, None])
+    total = int(sum(v.size for v in Vs))
+    g_stored = ctx.adjoint(gE, total)
+    s2 = ctx.solve(Vs, b.r_min, b.r_max, b.mu, b.e_cap, b.n_trial, method=method, level_capacity=cap)
+    g_recomp = ctx.adjoint(gE, total, recompute=True)
+    g_again = ctx.adjoint(gE, total, recompute=True)
+    assert np.array_equal(np.nan_to_num(s1.energy), np.nan_to_num(s2.energy))
+    scale = np.abs(g_stored).max()
+    assert np.max(np.abs(g_recomp - g_stored)) <= 1e-12 * scale
+    assert np.array_equal(g_recomp, g_again)
