@@ -393,7 +393,7 @@ def main():
         "speedup_vs_plain_fp64": value / plain_value,
         "stages_ms": {"prepare": st.ms_prepare, "scan32": st.ms_scan, "refine32": st.ms_refine32,
                       "polish64": st.ms_polish64, "write64": st.ms_write, "solve_total": st.ms_total,
-                      "fp64_fallbacks": st.fallbacks},
+                      "fallbacks": st.fallbacks, "twist_searches": st.twist_searches},
         "roofline": roof,
         "psi_write": {"bytes": st.psi_bytes, "GB_per_s": write_gbs, "hbm_peak_GBs": hbm},
         "e2e": {"value": e2e_good * world / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),

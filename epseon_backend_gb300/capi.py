@@ -107,6 +107,8 @@ class Stats(C.Structure):
         ("n_levels", C.c_int64),
         ("kernel_launches", C.c_int32),
         ("fallbacks", C.c_int32),
+        ("twist_searches", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 

@@ -610,6 +610,7 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     st.scan_point_updates = scan_pts;
     st.n_levels = nlev;
     st.fallbacks = hh->fallbacks;
+    st.twist_searches = hh->n_twist;
     st.psi_bytes = want_psi ? psi_total * 8 : 0;
     st.kernel_launches = 9 + (want_psi ? 1 : 0) + (method == EPSCU_METHOD_FAST_FP32C ? 2 : 0);
     if (method == EPSCU_METHOD_PLAIN_FP64) {

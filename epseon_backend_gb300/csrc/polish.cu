@@ -56,7 +56,6 @@ __device__ __forceinline__ void side_df(const float2* __restrict__ Wf, dfl aE, i
     dfl F = {0.0f, 0.0f};
     if (MODE == 2) F = df_from_double(L * ldexp(1.0, min(1000, max(-1100, -Xk))));
     const int nsteps = (to - from) * dir;
-    // two 8-point chunks of grid values in flight (register double buffer)
     auto load8 = [&](float2* w8, int base) {
 #pragma unroll
         for (int u = 0; u < 8; ++u) w8[u] = __ldg(Wf + from + dir * min(base + u, nsteps - 1));
@@ -121,14 +120,12 @@ __device__ __forceinline__ void side_df(const float2* __restrict__ Wf, dfl aE, i
             }
         }
         };
-    float2 wa[8], wb[8];
-    if (nsteps > 0) load8(wa, 0);
-    for (int base = 0; base < nsteps; base += 16) {
-        if (base + 8 < nsteps) load8(wb, base + 8);
-        run8(wa, base);
-        if (base + 8 >= nsteps) break;
-        if (base + 16 < nsteps) load8(wa, base + 16);
-        run8(wb, base + 8);
+    // one 8-point chunk in flight: the double-float body is long enough to hide
+    // the load behind the other resident warps (a second buffer costs occupancy)
+    for (int base = 0; base < nsteps; base += 8) {
+        float2 w8[8];
+        load8(w8, base);
+        run8(w8, base);
     }
     if (MODE == 1) st.S += f2d(Sacc.h) + f2d(Sacc.l);
 }
@@ -186,7 +183,7 @@ __device__ PassDF pass_df(const PotMeta& m, const float2* __restrict__ Wf, const
     return r;
 }
 
-__global__ void __launch_bounds__(kThreads) newton_df_kernel(DevBatch b) {
+__global__ void __launch_bounds__(kThreads, 4) newton_df_kernel(DevBatch b) {
     for (int2 unit; next_unit(b, kQNewtonDF, unit);) {
         if ((int)(threadIdx.x & 31) >= unit.y) continue;
         const int slot = unit.x + (threadIdx.x & 31);
@@ -294,7 +291,7 @@ __device__ __forceinline__ bool suspicious(const PotMeta& m, const LevelWork& w,
     return (nodes != w.v && !(m.status & EPSCU_STATUS_UNDER)) || !(fabs(dE) <= 1e-11 * fmax(1.0, fabs(w.E)));
 }
 
-__global__ void __launch_bounds__(kThreads) norm_df_kernel(DevBatch b) {
+__global__ void __launch_bounds__(kThreads, 4) norm_df_kernel(DevBatch b) {
     for (int2 unit; next_unit(b, kQNormDF, unit);) {
         if ((int)(threadIdx.x & 31) >= unit.y) continue;
         const int slot = unit.x + (threadIdx.x & 31);
@@ -409,7 +406,7 @@ __global__ void __launch_bounds__(64) twist_df_kernel(DevBatch b) {
     }
 }
 
-__global__ void __launch_bounds__(kThreads) write_df_kernel(DevBatch b) {
+__global__ void __launch_bounds__(kThreads, 4) write_df_kernel(DevBatch b) {
     if (!b.psi || b.hdr->error) return;
     for (int2 unit; next_unit(b, kQWriteDF, unit);) {
         if ((int)(threadIdx.x & 31) >= unit.y) continue;

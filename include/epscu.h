@@ -210,7 +210,9 @@ typedef struct epscu_stats {
     int64_t psi_bytes;             /* wavefunction bytes written */
     int64_t n_levels;              /* levels solved */
     int32_t kernel_launches;       /* kernels launched by the solve */
-    int32_t fallbacks;             /* levels that needed the FP64 bisection fallback */
+    int32_t fallbacks;             /* levels that needed the bisection fallback */
+    int32_t twist_searches;        /* levels re-matched by the twist-index search */
+    int32_t reserved;
 } epscu_stats;
 epscu_status epscu_last_stats(epscu_ctx* ctx, epscu_stats* stats);
 

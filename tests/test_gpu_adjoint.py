@@ -43,20 +43,24 @@ def test_parameter_gradients_match_fd(method):
     grad = Pr.grad.cpu().numpy()
     h = 1e-6
     checked = 0
+    # 1e-6 relative to the potential's gradient scale: a component that nearly
+    # cancels across levels sits below the finite-difference noise floor
+    # (energy error ~1e-14 against a difference of ~1e-9)
     for p in range(len(b)):
         for j in [0, 1, 2, 3, 4, 5]:
             if j >= 3 and P[p, j].item() == 0.0:
                 continue
+            # central differences with h = 1e-6 (absolute, FP64)
             Pp, Pm = P.clone(), P.clone()
-            scale = max(abs(P[p, j].item()), 1e-3)
-            Pp[p, j] += h * scale
-            Pm[p, j] -= h * scale
+            Pp[p, j] += h
+            Pm[p, j] -= h
             with torch.no_grad():
                 Lp, _ = _loss(Pp, Pt, b.kind, g, solver, w)
                 Lm, _ = _loss(Pm, Pt, b.kind, g, solver, w)
-            fd = (Lp.item() - Lm.item()) / (2 * h * scale)
+            fd = (Lp.item() - Lm.item()) / (2 * h)
             an = grad[p, j]
-            assert abs(an - fd) <= 1e-6 * max(abs(fd), 1e-12) + 1e-9 * abs(L.item()) / scale, (p, j, an, fd)
+            gscale = np.max(np.abs(grad[p, :6]))
+            assert abs(an - fd) <= 1e-6 * max(abs(fd), gscale), (p, j, an, fd, gscale)
             checked += 1
     assert checked >= 10
 

@@ -152,3 +152,45 @@ def test_adjoint_recompute_equals_stored(ctx, method):
     scale = np.abs(g_stored).max()
     assert np.max(np.abs(g_recomp - g_stored)) <= 1e-12 * scale
     assert np.array_equal(g_recomp, g_again)
+
+
+@pytest.mark.parametrize("method", [capi.METHOD_PLAIN_FP64, capi.METHOD_FAST_FP32C])
+def test_bump_wavefunctions_all_levels(ctx, method):
+    """Every level of Morse+bump potentials (double wells, near-degenerate
+    pairs): energies, node counts and psi against the oracle."""
+    b = synth.bump_adjoint(B=3, N=6144, n_trial=2048)
+    refs = _oracle(b, want_psi=True)
+    sol = _gpu(ctx, b, method, want_psi=True, cap=256)
+    for q, ref in enumerate(refs):
+        n = sol.n_out[q]
+        assert n == ref.n_total
+        assert np.array_equal(sol.nodes[q, :n], np.arange(n))
+        tol = E_TOL_PLAIN if method == capi.METHOD_PLAIN_FP64 else E_TOL_FAST
+        assert np.max(np.abs(sol.energy[q, :n] - ref.energy_polished)) < tol
+        psi = sol.wavefunctions(q)
+        errs = [_psi_l2(psi[v], ref.psi[v], ref.grid.h) for v in range(n)]
+        worst = int(np.argmax(errs))
+        assert errs[worst] < PSI_TOL, (q, worst, errs[worst])
+
+
+@pytest.mark.parametrize("method", [capi.METHOD_PLAIN_FP64, capi.METHOD_FAST_FP32C])
+def test_long_grid_top_levels(ctx, method):
+    """Long grid (one heavy Morse, N = 2^20, ~280 bound levels): the ten highest
+    levels (and the lowest three) against the oracle, with a reduced number of
+    trial energies so the oracle finishes in seconds."""
+    b = synth.morse_long(n_trial=4096)
+    V = b.V(0)
+    for lo, hi in ((0, 2), (270, 279)):
+        ref = O.solve_batch([V], b.r_min, b.r_max, b.mu, b.e_cap, b.n_trial, min_level=lo, max_level=hi,
+                            want_psi=True)[0]
+        assert ref.n_total == 280
+        sol = ctx.solve([V], b.r_min, b.r_max, b.mu, b.e_cap, b.n_trial, method=method, min_level=lo,
+                        max_level=hi, want_psi=True)
+        n = sol.n_out[0]
+        assert sol.n_total[0] == 280 and n == hi - lo + 1
+        assert np.array_equal(sol.nodes[0, :n], np.arange(lo, hi + 1))
+        tol = E_TOL_PLAIN if method == capi.METHOD_PLAIN_FP64 else E_TOL_FAST
+        assert np.max(np.abs(sol.energy[0, :n] - ref.energy_polished)) < tol
+        psi = sol.wavefunctions(0)
+        for s in range(n):
+            assert _psi_l2(psi[s], ref.psi[s], ref.grid.h) < PSI_TOL
