@@ -128,6 +128,7 @@ EXPORTED = [
     "epscu_cancel",
     "epscu_last_stats",
     "epscu_measure_fma_peaks",
+    "epscu_count_levels_static",
 ]
 
 _lib = None
@@ -168,6 +169,8 @@ def load(build_if_missing: bool = True):
     L.epscu_cancel.argtypes = [C.c_void_p]
     L.epscu_last_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
     L.epscu_measure_fma_peaks.argtypes = [C.c_void_p, _dp, _dp]
+    L.epscu_count_levels_static.argtypes = [_dp, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_double,
+                                            C.c_int32, _ip, C.c_void_p]
     for name in EXPORTED:
         if name not in ("epscu_abi_version", "epscu_last_error"):
             getattr(L, name).restype = C.c_int32

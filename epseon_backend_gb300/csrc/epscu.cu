@@ -58,6 +58,8 @@ constexpr int kStageEvents = 8;
 
 }  // namespace
 
+void epscu::set_last_error(const std::string& msg) { g_err = msg; }
+
 struct epscu_ctx {
     int device = 0;
     int sm_count = 0;

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 #include "common.cuh"
 
 namespace epscu {
@@ -92,6 +94,9 @@ void launch_adjoint(const DevBatch& b, const double* dL_dE, double* dL_dV, int64
 void launch_adjoint_explicit(int32_t n, int32_t cap, int32_t max_N, const int64_t* offsets, const int32_t* N,
                              const double* h, const int32_t* n_out, const int64_t* psi_off, const double* psi,
                              const double* gE, double* gV, cudaStream_t s);
+
+// epscu.cu: the calling thread's message for epscu_last_error()
+void set_last_error(const std::string& msg);
 
 // peaks.cu
 void measure_fma_peaks(int sm_count, double* fp32_tflops, double* fp64_tflops);

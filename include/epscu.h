@@ -220,6 +220,24 @@ epscu_status epscu_last_stats(epscu_ctx* ctx, epscu_stats* stats);
  * kernel (TFLOP/s, 2 flops per FMA).  Used for the roofline denominators. */
 epscu_status epscu_measure_fma_peaks(epscu_ctx* ctx, double* fp32_tflops, double* fp64_tflops);
 
+/* Level counting for one potential that allocates nothing.  Some callers
+ * cannot call cudaMalloc (a plugin inside another framework's memory pool or
+ * allocation budget, a context where allocation is not permitted); this entry
+ * point runs the trial-energy scan of epscu_solve on scratch held in a
+ * file-scope __device__ array of the library (about 1.5 MiB per device, kept
+ * until the process exits).  No counterpart in the reference.
+ *   V      : device pointer, N grid values (Hartree) on [r_min, r_max]
+ *   counts : device pointer, n_trial outputs: the number of bound levels below
+ *            E_j = min V + (j+1) (e_cap - min V) / n_trial
+ *   stream : cudaStream_t the work is queued on (NULL: legacy default stream);
+ *            the call returns without synchronising.
+ * Grids longer than 65536 points return EPSCU_ERR_CAPACITY.  The first call
+ * on each device looks up the scratch's device address (make it before any
+ * stream capture).  All calls share the scratch: calls that overlap on the GPU
+ * race and must be serialised by the caller. */
+epscu_status epscu_count_levels_static(const double* V, int32_t N, double r_min, double r_max, double mu,
+                                       double e_cap, int32_t n_trial, int32_t* counts, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
