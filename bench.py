@@ -48,11 +48,37 @@ def dist_env():
     return rank, world, local
 
 
-def workload(rank: int, **kw):
-    """Rank r solves its own seeded batch (independent potentials: weak scaling)."""
+WORKLOADS = {
+    "mixed": "mixed_batch: 2048 potentials (1/3 Morse, 1/3 LJ 12-6, 1/3 Morse+1-3 Gaussian bumps via 1024-knot "
+             "natural spline), N~logU[2048,65536], mu~logU[500,1e5], 8192 trial energies, levels up to 0.999 De, "
+             "psi written, adjoint dL/dV",
+    "single": "morse_single: one Morse (De=0.1, a=1, re=2, mu=1000) on N=4096, r in [0.5, 27], 1024 trial "
+              "energies, psi written, adjoint dL/dV",
+    "morse64": "morse_batch: 64 Morse, De~U[0.02,0.2], a~U[0.5,1.5], re~U[1.5,4], mu~logU[500,1e5], N=16384 on "
+               "[0.5, re+30/a], 8192 trial energies, psi written, adjoint dL/dV",
+    "adjoint256": "bump_adjoint: 256 Morse+1-3 Gaussian bumps (1024-knot spline) on N=32768, 8192 trial energies; "
+                  "loss sum_v w_v (E_v - T_v)^2, T_v = levels with bump amplitudes x1.1, w_v~U[0.5,1]",
+    "long": "morse_long: one Morse (De=0.15, a=0.6, re=4, mu=1e5) on N=2^20, r in [0.5, 54], 65536 trial "
+            "energies, psi written, adjoint dL/dV",
+}
+
+
+def workload(rank: int, name: str = "mixed", **kw):
+    """Rank r solves its own seeded batch (independent potentials: weak scaling).
+    The single-potential workloads are replicas (the same potential per rank)."""
     from epseon_backend_gb300 import synth
 
-    return synth.mixed_batch(seed=3 + 100 * rank, **kw)
+    if name == "mixed":
+        return synth.mixed_batch(seed=3 + 100 * rank, **kw)
+    if name == "morse64":
+        return synth.morse_batch(seed=2 + 100 * rank, **kw)
+    if name == "adjoint256":
+        return synth.bump_adjoint(seed=4 + 100 * rank, **kw)
+    if name == "single":
+        return synth.morse_single(**kw)
+    if name == "long":
+        return synth.morse_long(**kw)
+    raise ValueError(f"unknown workload {name!r}")
 
 
 def aggregate(ms_local: float, levels_local: int, dist=None, device=None):
@@ -170,7 +196,7 @@ def run_reference(args, rank, world):
     from oracle import build as ob
 
     ob.build()
-    b = workload(0)
+    b = workload(0, args.workload)
     cores = os.cpu_count() or 1
     for _ in range(args.warmup):
         cpu_oracle_leg(b, cores, seed=0)
@@ -180,7 +206,8 @@ def run_reference(args, rank, world):
         t_all += dt
         lev_all += levels
     v = lev_all / t_all
-    sample = f"{CPU_SAMPLE} of {len(b)} potentials of mixed_batch per step (random, seeded), plain FP64 method"
+    sample = (f"{min(CPU_SAMPLE, len(b))} of {len(b)} potentials of {args.workload} per step (random, seeded), "
+              "plain FP64 method")
     out = {
         "impl": "reference",
         "metric": METRIC,
@@ -195,8 +222,7 @@ def run_reference(args, rank, world):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded PCG64)",
-        "config": {"workload": "mixed_batch: 2048 Morse/LJ/Morse+bump potentials, N~logU[2048,65536], 8192 trial E",
-                   "sample": sample},
+        "config": {"workload": WORKLOADS[args.workload], "sample": sample},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -211,8 +237,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--batch", type=int, default=2048,
-                    help="potentials per GPU (2048 = the measured workload; smaller for profiler captures)")
+    ap.add_argument("--batch", type=int, default=None,
+                    help="potentials per GPU of the mixed workload (default 2048; smaller for profiler captures)")
+    ap.add_argument("--workload", default="mixed", choices=sorted(WORKLOADS),
+                    help="mixed = the headline batch; the others are the single-Morse, 64-Morse, adjoint and "
+                         "long-grid cases")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
@@ -236,7 +265,7 @@ def main():
 
     ctx = capi.Context(local)
     fp32_peak, fp64_peak = ctx.measure_fma_peaks()
-    b = workload(rank, B=args.batch)
+    b = workload(rank, args.workload, **({"B": args.batch} if args.batch else {}))
     Vs = b.potentials()
     cap = 512
 
@@ -269,7 +298,16 @@ def main():
     rng = np.random.default_rng(1000 + rank)
     w_np = rng.uniform(0.5, 1.0, (len(b), cap))
     w = torch.from_numpy(w_np).cuda()
-    target_np = np.nan_to_num(ref.energy, nan=0.0) * 1.001
+    if args.workload == "adjoint256":
+        # targets: the levels of the same potentials with every bump amplitude x1.1
+        from epseon_backend_gb300 import synth
+
+        tb = synth.bump_adjoint(seed=4 + 100 * rank, amp_scale=1.1)
+        tsol = ctx.solve(tb.potentials(), tb.r_min, tb.r_max, tb.mu, tb.e_cap, tb.n_trial,
+                         method=capi.METHOD_PLAIN_FP64, level_capacity=cap)
+        target_np = np.where(np.arange(cap)[None, :] < tsol.n_out[:, None], np.nan_to_num(tsol.energy), 0.0)
+    else:
+        target_np = np.nan_to_num(ref.energy, nan=0.0) * 1.001
     target = torch.from_numpy(target_np).cuda()
     slot = torch.arange(cap, device="cuda")[None, :]
     mask = (slot < n_lev[:, None]).to(torch.float64)
@@ -341,20 +379,20 @@ def main():
                "sample": f"{len(idx)} of {len(b)} potentials (seeded random), plain FP64 method, {dt:.1f} s",
                "plain_gpu_bit_exact_on_sample": bool(same)}
 
-    # ---- roofline of the dominant kernel stage
+    # ---- roofline of the dominant kernel: scan32 (the longest single launch;
+    # the per-level stages are split over several kernels each).  Unit: one
+    # Numerov point-update = 9 algorithmic flops (T, f, g, two-term recurrence);
+    # compensation, renormalisation and sign bookkeeping are not counted.
     scan_flops = 9.0 * st.scan_point_updates
-    stages = {"scan32": st.ms_scan, "refine32": st.ms_refine32, "polish64": st.ms_polish64, "write64": st.ms_write}
-    dom = max(stages, key=stages.get)
-    if dom == "scan32":
-        ach = scan_flops / (st.ms_scan * 1e-3) / 1e12
-        roof = {"bound": "fp32_alu", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s", "frac": ach / fp32_peak,
-                "traffic": None, "kernel": "scan32_kernel", "peak_source": "measured FMA burst (epscu_measure_fma_peaks)"}
-    else:
-        pts = st.fp64_point_updates
-        ms_stage = stages[dom]
-        ach = 9.0 * pts / (max(ms_stage, 1e-6) * 1e-3) / 1e12 if dom != "write64" else 9.0 * pts / 3 / (ms_stage * 1e-3) / 1e12
-        roof = {"bound": "fp64_alu", "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s", "frac": ach / fp64_peak,
-                "traffic": None, "kernel": dom, "peak_source": "measured FMA burst (epscu_measure_fma_peaks)"}
+    ach = scan_flops / (st.ms_scan * 1e-3) / 1e12
+    roof = {"bound": "fp32_alu", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s", "frac": ach / fp32_peak,
+            "traffic": None, "kernel": "scan32_kernel",
+            "algorithmic": {"point_updates": int(st.scan_point_updates), "flops_per_update": 9},
+            "peak_source": "measured FP32 FMA burst (epscu_measure_fma_peaks), 2 flops per FMA"}
+    # the FP64-pipe view of the plain solver's dominant kernel, for comparison
+    roof_plain = {"kernel": "scan64_kernel", "achieved": 9.0 * plain_stats.scan_point_updates
+                  / (plain_stats.ms_scan * 1e-3) / 1e12, "peak": fp64_peak, "unit": "TFLOP/s"}
+    roof_plain["frac"] = roof_plain["achieved"] / fp64_peak
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs")
     write_gbs = (st.psi_bytes / (st.ms_write * 1e-3) / 1e9) if st.ms_write > 0 else None
@@ -375,9 +413,7 @@ def main():
         "dtype": "f32+f64",
         "data": "synthetic (seeded PCG64 potentials; no dataset)",
         "config": {
-            "workload": "mixed_batch: 2048 potentials (1/3 Morse, 1/3 LJ 12-6, 1/3 Morse+1-3 Gaussian bumps via "
-                        "1024-knot natural spline), N~logU[2048,65536], mu~logU[500,1e5], 8192 trial energies, "
-                        "levels up to 0.999 De, psi written, adjoint dL/dV",
+            "workload": WORKLOADS[args.workload],
             "potentials_per_gpu": len(b),
             "grid_points_per_gpu": int(b.N.sum()),
             "levels_per_gpu": total,
@@ -395,6 +431,7 @@ def main():
                       "polish64": st.ms_polish64, "write64": st.ms_write, "solve_total": st.ms_total,
                       "fallbacks": st.fallbacks, "twist_searches": st.twist_searches},
         "roofline": roof,
+        "roofline_plain_fp64": roof_plain,
         "psi_write": {"bytes": st.psi_bytes, "GB_per_s": write_gbs, "hbm_peak_GBs": hbm},
         "e2e": {"value": e2e_good * world / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
