@@ -1,0 +1,60 @@
+// dfpass.cuh -- pieces shared by the double-float passes of the fast method
+// (polish.cu: one lane per level; longwin.cu: one CTA per long level).
+#pragma once
+
+#include <math.h>
+
+#include "common.cuh"
+#include "dfloat.cuh"
+
+namespace epscu {
+
+// Windows longer than this many points take the CTA-per-level passes of
+// longwin.cu (parallel prefix over chunks) instead of one lane per level.
+constexpr int kLongWindow = 65536;
+
+__device__ __forceinline__ bool is_long(const LevelWork& w) { return w.j1 - w.j0 > kLongWindow; }
+
+// match points stay inside the level's window, off its two end points
+__device__ __forceinline__ int clamp_k(const LevelWork& w, int k) { return max(w.j0 + 1, min(k, w.j1 - 1)); }
+
+__device__ __forceinline__ dfl energy_df(const PotMeta& m, double E) {
+    return df_from_double(__dmul_rn(m.a, E));
+}
+
+struct PassDF {
+    double dE, gamma, sum;
+    double pk_out, pk_in;
+    int ex_out, ex_in;
+    int nodes, count;
+    int peak_i, peak_log2;
+};
+
+// Write the normalisation constants of pass r (match point k) into w.
+__device__ __forceinline__ void finalize_df(const PotMeta& m, LevelWork& w, const PassDF& r, int k) {
+    double ck = 1.0 / sqrt(m.h * r.sum);
+    if (r.pk_out < 0.0) ck = -ck;  // psi > 0 next to the inner wall
+    w.k = k;
+    w.ck = ck;
+    w.norm_k_out = ck / r.pk_out;
+    w.norm_k_in = ck / r.pk_in;
+    w.ex_out = r.ex_out;
+    w.ex_in = r.ex_in;
+    w.dE = r.dE;
+    w.nodes = r.nodes;
+    w.status &= ~EPSCU_STATUS_NOTFOUND;
+    if (!isfinite(r.dE) || !isfinite(ck)) w.status |= EPSCU_STATUS_NONFINITE;
+    if (r.nodes != w.v && !(m.status & EPSCU_STATUS_UNDER)) w.status |= EPSCU_STATUS_NOTFOUND;
+}
+
+// a converged level whose final pass disagrees (node count, or a Cooley
+// correction far above the energy's accuracy) was matched at a poor point
+__device__ __forceinline__ bool suspicious(const PotMeta& m, const LevelWork& w, int nodes, double dE) {
+    return (nodes != w.v && !(m.status & EPSCU_STATUS_UNDER)) || !(fabs(dE) <= 1e-11 * fmax(1.0, fabs(w.E)));
+}
+
+__device__ __forceinline__ bool no_result(const LevelWork& w) {
+    return (w.status & (EPSCU_STATUS_NOTFOUND | EPSCU_STATUS_CANCELLED | EPSCU_STATUS_NONFINITE)) != 0;
+}
+
+}  // namespace epscu

@@ -286,8 +286,12 @@ void enqueue_pipeline(epscu_ctx* ctx, const DevBatch& b, int method, bool want_p
     rec(0);
     launch_prepare(b, s);
     rec(1);
-    if (method == EPSCU_METHOD_PLAIN_FP64) launch_scan64(b, s);
-    else launch_scan32(b, shape, ctx->sm_count, s);
+    if (method == EPSCU_METHOD_PLAIN_FP64) {
+        launch_scan64(b, s);
+    } else {
+        launch_scan_window(b, ctx->sm_count, s);
+        launch_scan32(b, shape, ctx->sm_count, s);
+    }
     rec(2);
     launch_level_setup(b, s);
     if (method == EPSCU_METHOD_PLAIN_FP64) {
@@ -298,14 +302,20 @@ void enqueue_pipeline(epscu_ctx* ctx, const DevBatch& b, int method, bool want_p
         rec(4);
         if (want_psi) launch_write64(b, ctx->sm_count, s);
     } else {
+        launch_window(b, ctx->sm_count, s);
         launch_refine32(b, ctx->sm_count, s);
+        launch_refine_long(b, ctx->sm_count, s);
         rec(3);
         launch_newton_df(b, ctx->sm_count, s);
         launch_fallback_df(b, ctx->sm_count, s);
         launch_norm_df(b, ctx->sm_count, s);
+        launch_norm_long(b, ctx->sm_count, s);
         launch_twist_df(b, ctx->sm_count, s);
         rec(4);
-        if (want_psi) launch_write_df(b, ctx->sm_count, s);
+        if (want_psi) {
+            launch_write_df(b, ctx->sm_count, s);
+            launch_write_long(b, ctx->sm_count, s);
+        }
     }
     rec(5);
 }
@@ -403,6 +413,15 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     b.twist_list = (int32_t*)ctx->get("twist_list", sizeof(int32_t) * b.max_twist, &ce);
     b.hdr = (Header*)ctx->get("hdr", sizeof(Header), &ce);
     b.order = (int32_t*)ctx->get("order", sizeof(int32_t) * n, &ce);
+    b.scan_win = nullptr;
+    b.long_list = nullptr;
+    if (method == EPSCU_METHOD_FAST_FP32C) {
+        b.long_list = (int32_t*)ctx->get("long_list", sizeof(int32_t) * lv, &ce);
+        if (!b.long_list) return fail(EPSCU_ERR_NOMEM, "device arena (long list)");
+        const size_t nb = (size_t)(batch->n_trial + kScanWinBlock - 1) / kScanWinBlock;
+        b.scan_win = (int2*)ctx->get("scan_win", sizeof(int2) * (size_t)n * nb, &ce);
+        if (!b.scan_win) return fail(EPSCU_ERR_NOMEM, "device arena (scan windows)");
+    }
     int64_t* d_off = (int64_t*)ctx->get("offsets", sizeof(int64_t) * n, &ce);
     if (ce != cudaSuccess || !b.meta || !b.W64 || !b.Msuf || !b.counts || !b.levels || !b.fallback_list || !b.units ||
         !b.hdr ||
@@ -477,6 +496,7 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
         EPSCU_CU(cudaMemsetAsync(b.Wf2, 0, sizeof(float2) * total_padded, s));
         EPSCU_CU(cudaMemsetAsync(b.hdr, 0, sizeof(Header), s));
         launch_prepare(b, s);
+        launch_scan_window(b, ctx->sm_count, s);
         const ScanShape cands[] = {{128, 1024, 4, 0}, {128, 2048, 3, 0}, {256, 1024, 4, 0}, {256, 2048, 3, 0},
                                    {256, 4096, 2, 0}, {512, 1024, 4, 0}, {512, 2048, 3, 0}};
         float best = 1e30f;
@@ -609,7 +629,8 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
         lvl_pts += interior * hm[p].n_out;
         nlev += hm[p].n_out;
     }
-    st.scan_point_updates = scan_pts;
+    // the windowed FP32 scan counts what it did; the FP64 scan covers [i0, i1]
+    st.scan_point_updates = hh->scan_updates > 0 ? (int64_t)hh->scan_updates : scan_pts;
     st.n_levels = nlev;
     st.fallbacks = hh->fallbacks;
     st.twist_searches = hh->n_twist;
@@ -666,8 +687,12 @@ extern "C" epscu_status epscu_adjoint(epscu_ctx* ctx, const double* dL_dE, doubl
         // the writer of the solve's own method (its norm constants belong to it)
         const int qid = ctx->last_method == EPSCU_METHOD_FAST_FP32C ? kQWriteDF : kQWrite64;
         EPSCU_CU(cudaMemsetAsync(&b.hdr->queue[qid], 0, sizeof(int32_t), s));
-        if (ctx->last_method == EPSCU_METHOD_FAST_FP32C) launch_write_df(b, ctx->sm_count, s);
-        else launch_write64(b, ctx->sm_count, s);
+        if (ctx->last_method == EPSCU_METHOD_FAST_FP32C) {
+            launch_write_df(b, ctx->sm_count, s);
+            launch_write_long(b, ctx->sm_count, s);
+        } else {
+            launch_write64(b, ctx->sm_count, s);
+        }
     }
     const bool dev = (opts.flags & EPSCU_MEM_DEVICE) != 0;
     const int64_t lv = (int64_t)b.n * b.level_capacity;

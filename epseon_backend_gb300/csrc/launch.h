@@ -30,6 +30,8 @@ struct DevBatch {
     int32_t level_capacity;    // slots per potential
     Header* hdr;
     int32_t* order;            // [n] potentials by decreasing cost
+    int2* scan_win;            // [n * ceil(n_trial / kScanWinBlock)] scan windows, or nullptr (full grid)
+    int32_t* long_list;        // [max_levels] slots with long windows (CTA-per-level passes), or nullptr
     double* psi;               // compact wavefunctions or nullptr
     int64_t psi_capacity;
     volatile int32_t* cancel;  // host-mapped cancel flag (device pointer) or nullptr
@@ -54,6 +56,8 @@ __device__ __forceinline__ bool next_unit(const DevBatch& b, int qid, int2& unit
 // prepare.cu
 void launch_prepare(const DevBatch& b, cudaStream_t s);
 void launch_level_setup(const DevBatch& b, cudaStream_t s);
+void launch_window(const DevBatch& b, int sm_count, cudaStream_t s);
+void launch_scan_window(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_tabulate(int32_t n, const int32_t* kind, const double* params, const int64_t* offsets,
                      const int32_t* N, const double* r_min, const double* r_max, int32_t n_knots,
                      double* knot_scratch, double* V, cudaStream_t s);
@@ -86,6 +90,11 @@ void launch_write_df(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_fallback_df(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_twist_df(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_twist64(const DevBatch& b, int sm_count, cudaStream_t s);
+
+// longwin.cu
+void launch_refine_long(const DevBatch& b, int sm_count, cudaStream_t s);
+void launch_norm_long(const DevBatch& b, int sm_count, cudaStream_t s);
+void launch_write_long(const DevBatch& b, int sm_count, cudaStream_t s);
 
 // adjoint.cu
 void launch_adjoint(const DevBatch& b, const double* dL_dE, double* dL_dV, int64_t total_points,

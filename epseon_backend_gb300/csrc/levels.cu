@@ -27,6 +27,7 @@
 #include <stdint.h>
 
 #include "common.cuh"
+#include "dfpass.cuh"
 #include "launch.h"
 
 namespace epscu {
@@ -221,16 +222,16 @@ struct Pass32 {
 };
 
 __device__ __forceinline__ Pass32 cooley32(const PotMeta& m, const float2* __restrict__ Wf, const double* __restrict__ W64,
-                                           double E, int k) {
+                                           double E, int k, int j0, int j1) {
     const double aE = __dmul_rn(m.a, E);
     const float aEh = __double2float_rn(aE);
     const float aEl = __double2float_rn(aE - (double)aEh);
     float Ao = 1.f, Do = 1.f, So = 0.f, Ai = 1.f, Di = 1.f, Si = 0.f;
-    int Lk[2] = {0, 0}, Lpk[2] = {-(1 << 30), -(1 << 30)}, ipk[2] = {m.i0, m.i1};
+    int Lk[2] = {0, 0}, Lpk[2] = {-(1 << 30), -(1 << 30)}, ipk[2] = {j0, j1};
     int nodes = 0;
     for (int side = 0; side < 2; ++side) {
         float A = 1.0f, D = 1.0f, S = 0.0f;
-        const int from = side == 0 ? m.i0 : m.i1;
+        const int from = side == 0 ? j0 : j1;
         const int to = k;
         const int dir = side == 0 ? 1 : -1;
         int ecum = 0;
@@ -322,7 +323,7 @@ __global__ void __launch_bounds__(kLevelThreads) refine32_kernel(DevBatch b) {
         if ((int)(threadIdx.x & 31) >= unit.y) continue;
         const int slot = unit.x + (threadIdx.x & 31);
         LevelWork w = b.levels[slot];
-        if (w.status & EPSCU_STATUS_NOTFOUND) continue;
+        if ((w.status & EPSCU_STATUS_NOTFOUND) || is_long(w)) continue;  // long windows: refine_long
         if (cancelled(b)) {
             b.levels[slot].status = w.status | EPSCU_STATUS_CANCELLED;
             continue;
@@ -331,29 +332,41 @@ __global__ void __launch_bounds__(kLevelThreads) refine32_kernel(DevBatch b) {
         const float2* Wf = b.Wf2 + m.offf;
         const double* W64 = b.W64 + m.off;
         double lo = w.lo, hi = w.hi, E = w.E;
-        int k = clamp_inner(m, match_index(m, b.Msuf, E));
+        // the level's window (decay window of its bracket)
+        auto clamp_w = [&](int kk) { return max(w.j0 + 1, min(kk, w.j1 - 1)); };
+        int k = clamp_w(match_index(m, b.Msuf, E));
         bool bisect = false, confirming = false, done = false;
         double E_star = E, sum = 1.0;
         int it = 0;
-        for (; it < 48; ++it) {
-            const Pass32 r = cooley32(m, Wf, W64, E, k);
+        int k_sum = k;  // match point of `sum` (sum psi~^2 is normalised by psi at k)
+        // the Newton stage divides by sum psi~^2 at the final match point: when
+        // the deciding pass moved the match point, one more pass at E_star
+        // recomputes the sum there (a stale sum is off by (psi_k_old/psi_k)^2
+        // and slows Newton to a crawl)
+        bool final_pass = false;
+        for (; it < 48 || final_pass; ++it) {
+            const Pass32 r = cooley32(m, Wf, W64, E, k, w.j0, w.j1);
+            sum = r.sum;
+            k_sum = k;
+            if (final_pass) break;
             if (r.count > w.v) hi = E;
             else lo = E;
-            sum = r.sum;
             const bool moved = r.peak_log2 >= kPeakLog2;
-            if (moved) k = clamp_inner(m, r.peak_i);
+            if (moved) k = clamp_w(r.peak_i);
             if (confirming) {
                 confirming = false;
-                if (hi - lo <= 3.0 * kTol32 + 1e-15 && E_star >= lo && E_star <= hi) {
-                    done = true;
-                    break;
-                }
-                bisect = true;  // the predicted root was not confirmed
+                if (hi - lo <= 3.0 * kTol32 + 1e-15 && E_star >= lo && E_star <= hi) done = true;
+                else bisect = true;  // the predicted root was not confirmed
             }
-            if (hi - lo <= 2.0 * kTol32) {
+            if (!done && hi - lo <= 2.0 * kTol32) {
                 E_star = 0.5 * (lo + hi);
                 done = true;
-                break;
+            }
+            if (done) {
+                if (k == k_sum) break;
+                final_pass = true;
+                E = E_star;
+                continue;
             }
             double En;
             if (!bisect && !moved) {
@@ -379,7 +392,7 @@ __global__ void __launch_bounds__(kLevelThreads) refine32_kernel(DevBatch b) {
         w.hi = hi;
         w.E = E_star;
         w.k = k;
-        w.norm_k_in = sum;  // sum psi~^2 of the last pass, the Newton denominator of newton64
+        w.norm_k_in = sum;  // sum psi~^2 at the match point k, the Newton denominator of newton_df
         w.iters = it;
         b.levels[slot] = w;
     }

@@ -1,0 +1,567 @@
+// longwin.cu -- the fast method's per-level passes for long windows.
+//
+// A level whose window holds more than kLongWindow points (a long grid: the
+// 2^20-point Morse has windows of 10^5 - 4.7 10^5 points) cannot be marched
+// by one lane: a pass would cost ~10^6 dependent steps of latency while most
+// of the GPU idles.  Such a level takes one CTA of kLongThreads threads
+// instead.  Each side of a pass (outward from j0 to the match point k, inward
+// from j1 to k) is split into one contiguous chunk per thread and the
+// double-float difference-form recurrence
+//     D' = D + T (D - 12 A),   A' = A + (T A + D')
+// runs in three phases:
+//   1. every thread marches the two unit states (A, D) = (1, 0) and (0, 1)
+//      through its chunk: the step is linear in (A, D), so these are the
+//      columns of the chunk's 2x2 transfer matrix (with the product of 1/f
+//      over the chunk for the passes that need psi);
+//   2. a parallel prefix scan of the transfer matrices -- Hillis-Steele over
+//      the 32 lanes of each warp with shuffles, then over the warps through
+//      shared memory -- gives the exact starting state and scale of every
+//      chunk;
+//   3. every thread re-runs its chunk from that state: node counts, the sum
+//      of psi^2, the peak of |psi| or the psi write, reduced over the CTA.
+// A pass costs about three serial marches of point-updates, spread over
+// kLongThreads threads.  The matrices span exponential growth, so every
+// product is renormalised by a power of two with the exponent carried in an
+// int; the physical solution is the growing one on both sides (each side runs
+// from a forbidden region towards the match point at the peak of |psi|), so a
+// product applied to the starting state loses nothing to the discarded
+// subdominant solution.
+//
+// Kernels (one CTA per long level, levels from the long list the window
+// kernel fills; the lane-per-level kernels skip these levels):
+//   refine_long : safeguarded Cooley-Newton in double-float from the scan
+//                 bracket to 1e-12 (replaces refine32 + newton_df + fallback);
+//   norm_long   : the norm pass and its match-point candidates (as norm_df);
+//   write_long  : psi to HBM (as write_df).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "dfloat.cuh"
+#include "dfpass.cuh"
+#include "launch.h"
+
+namespace epscu {
+
+namespace {
+
+constexpr int kLongThreads = 256;
+constexpr int kLongWarps = kLongThreads / 32;
+
+// [[a, b], [c, d]] 2^e acting on the column (A, D)
+struct Mat2 {
+    dfl a, b, c, d;
+    int e;
+};
+
+// v 2^e
+struct Scal {
+    dfl v;
+    int e;
+};
+
+__device__ __forceinline__ Mat2 mat_identity() {
+    return {{1.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {1.0f, 0.0f}, 0};
+}
+
+__device__ __forceinline__ void mat_norm(Mat2& m) {
+    const float mm = fmaxf(fmaxf(fabsf(m.a.h), fabsf(m.b.h)), fmaxf(fabsf(m.c.h), fabsf(m.d.h)));
+    if (mm > 0.0f && mm < INFINITY) {
+        const int e = max(-120, min(120, fexp(mm)));
+        const float sc = fpow2(-e);
+        m.a = df_scale(m.a, sc);
+        m.b = df_scale(m.b, sc);
+        m.c = df_scale(m.c, sc);
+        m.d = df_scale(m.d, sc);
+        m.e += e;
+    }
+}
+
+// x y (x applied after y)
+__device__ __forceinline__ Mat2 mat_mul(const Mat2& x, const Mat2& y) {
+    Mat2 r;
+    r.a = df_add(df_mul(x.a, y.a), df_mul(x.b, y.c));
+    r.b = df_add(df_mul(x.a, y.b), df_mul(x.b, y.d));
+    r.c = df_add(df_mul(x.c, y.a), df_mul(x.d, y.c));
+    r.d = df_add(df_mul(x.c, y.b), df_mul(x.d, y.d));
+    r.e = x.e + y.e;
+    mat_norm(r);
+    return r;
+}
+
+__device__ __forceinline__ void scal_norm(Scal& s) {
+    const float mm = fabsf(s.v.h);
+    if (mm > 0.0f && mm < INFINITY) {
+        const int e = max(-120, min(120, fexp(mm)));
+        s.v = df_scale(s.v, fpow2(-e));
+        s.e += e;
+    }
+}
+
+__device__ __forceinline__ Scal scal_mul(const Scal& x, const Scal& y) {
+    Scal r{df_mul(x.v, y.v), x.e + y.e};
+    scal_norm(r);
+    return r;
+}
+
+__device__ __forceinline__ dfl shfl_up_df(dfl v, int o) {
+    return {__shfl_up_sync(0xffffffffu, v.h, o), __shfl_up_sync(0xffffffffu, v.l, o)};
+}
+
+__device__ __forceinline__ Mat2 shfl_up_mat(const Mat2& m, int o) {
+    return {shfl_up_df(m.a, o), shfl_up_df(m.b, o), shfl_up_df(m.c, o), shfl_up_df(m.d, o),
+            __shfl_up_sync(0xffffffffu, m.e, o)};
+}
+
+__device__ __forceinline__ Scal shfl_up_scal(const Scal& s, int o) {
+    return {shfl_up_df(s.v, o), __shfl_up_sync(0xffffffffu, s.e, o)};
+}
+
+// T = aE - W as a double-float (the same operations as the lane passes)
+__device__ __forceinline__ dfl t_of(dfl aE, float2 w) {
+    const dfl T = two_sum(aE.h, -w.x);
+    return fast_two_sum(T.h, __fadd_rn(T.l, __fsub_rn(aE.l, w.y)));
+}
+
+__device__ __forceinline__ void df_step(dfl T, dfl& A, dfl& D) {
+    const dfl X = df_add(D, df_mulf(A, -12.0f));
+    D = df_add(D, df_mul(T, X));
+    A = df_add(A, df_add(df_mul(T, A), D));
+}
+
+struct LongShared {
+    Mat2 wtot[kLongWarps], wpre[kLongWarps];
+    Scal qtot[kLongWarps], qpre[kLongWarps];
+    int nodes[kLongWarps];
+    double S[kLongWarps];
+    int pk_L[kLongWarps], pk_s[kLongWarps];
+    // the side's final state (written by the thread holding the last chunk)
+    dfl A, D, q;
+    int eA, eQ;
+};
+
+// One side of a pass over steps 0..nsteps-1 (point from + dir * step), the
+// CTA-parallel twin of side_df<MODE>: the same outputs in the same scales
+// (state and psi-hat at the end with their exponents, S relative to the
+// final scale, peak in absolute log2).  Called by every thread of the CTA.
+template <int MODE>
+struct LongSide {
+    dfl A, D, q;
+    int eA, eQ;
+    int nodes;
+    double S;
+    int peak_L, peak_i;
+};
+
+template <int MODE>
+__device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int from, int to, int dir,
+                                    double* __restrict__ out, double L, int Xk, LongShared& sh) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nsteps = (to - from) * dir;
+    LongSide<MODE> res;
+    if (nsteps <= 0) {
+        res.A = {1.0f, 0.0f};
+        res.D = {1.0f, 0.0f};
+        res.q = {1.0f, 0.0f};
+        res.eA = res.eQ = 0;
+        res.nodes = 0;
+        res.S = 0.0;
+        res.peak_L = -(1 << 30);
+        res.peak_i = from;
+        return res;
+    }
+    const int len = (nsteps + kLongThreads - 1) / kLongThreads;
+    const int s0 = min(tid * len, nsteps), s1 = min(s0 + len, nsteps);
+
+    // ---- phase 1: this chunk's transfer matrix (and product of 1/f)
+    Mat2 M;
+    Scal P{{1.0f, 0.0f}, 0};
+    {
+        dfl A1 = {1.0f, 0.0f}, D1 = {0.0f, 0.0f}, A2 = {0.0f, 0.0f}, D2 = {1.0f, 0.0f};
+        int e = 0;
+        for (int st = s0; st < s1; ++st) {
+            const dfl T = t_of(aE, __ldg(Wf + from + dir * st));
+            if (MODE >= 1) P.v = df_mul(P.v, df_recip(df_add({1.0f, 0.0f}, T)));
+            df_step(T, A1, D1);
+            df_step(T, A2, D2);
+            if (((st - s0) & 7) == 7) {
+                const float mm = fmaxf(fmaxf(fabsf(A1.h), fabsf(D1.h)), fmaxf(fabsf(A2.h), fabsf(D2.h)));
+                if (mm > 0.0f && mm < INFINITY) {
+                    const int ee = max(-120, min(120, fexp(mm)));
+                    const float sc = fpow2(-ee);
+                    A1 = df_scale(A1, sc);
+                    D1 = df_scale(D1, sc);
+                    A2 = df_scale(A2, sc);
+                    D2 = df_scale(D2, sc);
+                    e += ee;
+                }
+                if (MODE >= 1) scal_norm(P);
+            }
+        }
+        M = {A1, A2, D1, D2, e};
+        mat_norm(M);
+        if (MODE >= 1) scal_norm(P);
+    }
+
+    // ---- phase 2: exclusive prefix of the transfer matrices (later chunks on the left)
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const Mat2 y = shfl_up_mat(M, o);
+        const Scal py = shfl_up_scal(P, o);
+        if (lane >= o) {
+            M = mat_mul(M, y);
+            if (MODE >= 1) P = scal_mul(P, py);
+        }
+    }
+    if (lane == 31) {
+        sh.wtot[warp] = M;
+        sh.qtot[warp] = P;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        Mat2 acc = mat_identity();
+        Scal qa{{1.0f, 0.0f}, 0};
+        for (int w = 0; w < kLongWarps; ++w) {
+            sh.wpre[w] = acc;
+            sh.qpre[w] = qa;
+            acc = mat_mul(sh.wtot[w], acc);
+            if (MODE >= 1) qa = scal_mul(sh.qtot[w], qa);
+        }
+    }
+    __syncthreads();
+    Mat2 Mx = shfl_up_mat(M, 1);
+    Scal Px = shfl_up_scal(P, 1);
+    if (lane == 0) {
+        Mx = sh.wpre[warp];
+        Px = sh.qpre[warp];
+    } else {
+        Mx = mat_mul(Mx, sh.wpre[warp]);
+        if (MODE >= 1) Px = scal_mul(Px, sh.qpre[warp]);
+    }
+
+    // ---- phase 3: this chunk from its starting state (A, D) = Mx (1, 1)
+    dfl A = df_add(Mx.a, Mx.b), D = df_add(Mx.c, Mx.d);
+    int eA = Mx.e;
+    {
+        const float mm = fmaxf(fabsf(A.h), fabsf(D.h));
+        if (mm > 0.0f && mm < INFINITY) {
+            const int e = max(-120, min(120, fexp(mm)));
+            const float sc = fpow2(-e);
+            A = df_scale(A, sc);
+            D = df_scale(D, sc);
+            eA += e;
+        }
+    }
+    dfl q = Px.v;
+    int eQ = Px.e;
+    int nodes = 0;
+    double S = 0.0;
+    dfl Sacc = {0.0f, 0.0f};
+    int peak_L = -(1 << 30), peak_s = 0x7fffffff;
+    dfl F = {0.0f, 0.0f};
+    if (MODE == 2) F = df_from_double(L * ldexp(1.0, min(1000, max(-1100, eA + eQ - Xk))));
+    for (int st = s0; st < s1; ++st) {
+        const int i = from + dir * st;
+        const dfl T = t_of(aE, __ldg(Wf + i));
+        if (MODE >= 1) {
+            const dfl f = df_add({1.0f, 0.0f}, T);
+            const dfl qn = df_mul(q, df_recip(f));
+            const dfl psi = df_mul(A, qn);
+            if (MODE == 1) {
+                const float p = __fmul_rn(psi.h, psi.h);
+                const float e = __fmaf_rn(psi.h, psi.h, -p);
+                Sacc = df_add(Sacc, {p, __fmaf_rn(2.0f * psi.h, psi.l, e)});
+            } else {
+                const dfl v = df_mul(psi, F);
+                out[i] = f2d(v.h) + f2d(v.l);
+            }
+            q = qn;
+        }
+        const dfl X = df_add(D, df_mulf(A, -12.0f));
+        D = df_add(D, df_mul(T, X));
+        const dfl An = df_add(A, df_add(df_mul(T, A), D));
+        nodes += (__float_as_uint(An.h) ^ __float_as_uint(A.h)) >> 31;
+        A = An;
+        if (((st - s0) & 7) == 7 || st == s1 - 1) {
+            const float mm = fmaxf(fabsf(A.h), fabsf(D.h));
+            int e = 0, eq = 0;
+            if (mm > 0.0f && mm < INFINITY) {
+                e = max(-120, min(120, fexp(mm)));
+                const float sc = fpow2(-e);
+                A = df_scale(A, sc);
+                D = df_scale(D, sc);
+                eA += e;
+            }
+            if (MODE >= 1) {
+                eq = max(-120, min(120, fexp(q.h)));
+                q = df_scale(q, fpow2(-eq));
+                eQ += eq;
+                if (MODE == 1) {
+                    S = (S + (f2d(Sacc.h) + f2d(Sacc.l))) * ldexp(1.0, -2 * (e + eq));
+                    Sacc = {0.0f, 0.0f};
+                    const float mag = fabsf(__fmul_rn(A.h, q.h));
+                    if (mag > 0.0f) {
+                        const int Lm = fexp(mag) + eA + eQ;
+                        if (Lm > peak_L) {
+                            peak_L = Lm;
+                            peak_s = st;
+                        }
+                    }
+                } else if (e + eq != 0) {
+                    F = df_from_double(L * ldexp(1.0, min(1000, max(-1100, eA + eQ - Xk))));
+                }
+            }
+        }
+    }
+
+    // ---- reductions over the CTA
+    const int t_last = (nsteps - 1) / len;
+    if (tid == t_last) {
+        sh.A = A;
+        sh.D = D;
+        sh.q = q;
+        sh.eA = eA;
+        sh.eQ = eQ;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nodes += __shfl_xor_sync(0xffffffffu, nodes, o);
+    if (MODE == 1) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const int L2 = __shfl_xor_sync(0xffffffffu, peak_L, o);
+            const int s2 = __shfl_xor_sync(0xffffffffu, peak_s, o);
+            if (L2 > peak_L || (L2 == peak_L && s2 < peak_s)) {
+                peak_L = L2;
+                peak_s = s2;
+            }
+        }
+    }
+    if (lane == 0) {
+        sh.nodes[warp] = nodes;
+        sh.pk_L[warp] = peak_L;
+        sh.pk_s[warp] = peak_s;
+    }
+    __syncthreads();
+    res.A = sh.A;
+    res.D = sh.D;
+    res.q = sh.q;
+    res.eA = sh.eA;
+    res.eQ = sh.eQ;
+    if (MODE == 1) {
+        // this chunk's sum in the side's final scale
+        const int d = 2 * (eA + eQ - (res.eA + res.eQ));
+        double term = (s1 > s0 && d > -1000) ? S * ldexp(1.0, min(d, 1000)) : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) term += __shfl_xor_sync(0xffffffffu, term, o);
+        if (lane == 0) sh.S[warp] = term;
+    }
+    __syncthreads();
+    int nsum = 0;
+    double Ssum = 0.0;
+    int pL = -(1 << 30), ps = 0x7fffffff;
+    for (int w = 0; w < kLongWarps; ++w) {
+        nsum += sh.nodes[w];
+        if (MODE == 1) {
+            Ssum += sh.S[w];
+            if (sh.pk_L[w] > pL || (sh.pk_L[w] == pL && sh.pk_s[w] < ps)) {
+                pL = sh.pk_L[w];
+                ps = sh.pk_s[w];
+            }
+        }
+    }
+    res.nodes = nsum;
+    res.S = Ssum;
+    res.peak_L = pL;
+    res.peak_i = ps == 0x7fffffff ? from : from + dir * ps;
+    __syncthreads();  // the shared scratch is reused by the next call
+    return res;
+}
+
+// One pass at E with match point k (the CTA twin of pass_df<MODE>, MODE 0/1).
+template <int MODE>
+__device__ PassDF long_pass(const PotMeta& m, const LevelWork& w, const float2* __restrict__ Wf,
+                            const double* __restrict__ W64, double E, int k, double sum_fallback, LongShared& sh) {
+    const dfl aE = energy_df(m, E);
+    const LongSide<MODE> o = long_side<MODE>(Wf, aE, w.j0, k, +1, nullptr, 0.0, 0, sh);
+    const LongSide<MODE> in = long_side<MODE>(Wf, aE, w.j1, k, -1, nullptr, 0.0, 0, sh);
+    const double Tk = __dsub_rn(__dmul_rn(m.a, E), __ldg(W64 + k));
+    const double fk = 1.0 + Tk;
+    const double Ao = df_to_double(o.A), Do = df_to_double(o.D);
+    const double Ai = df_to_double(in.A), Di = df_to_double(in.D);
+    PassDF r;
+    r.gamma = -12.0 * Tk / fk + Do / Ao + Di / Ai;
+    r.nodes = o.nodes + in.nodes;
+    r.count = r.nodes + (r.gamma < 0.0 ? 1 : 0);
+    r.peak_i = k;
+    r.peak_log2 = 0;
+    r.pk_out = r.pk_in = 0.0;
+    r.ex_out = r.ex_in = 0;
+    if (MODE == 1) {
+        const double rfk = 1.0 / fk;
+        r.pk_out = Ao * df_to_double(o.q) * rfk;
+        r.pk_in = Ai * df_to_double(in.q) * rfk;
+        r.ex_out = o.eA + o.eQ;
+        r.ex_in = in.eA + in.eQ;
+        r.sum = o.S / (r.pk_out * r.pk_out) + in.S / (r.pk_in * r.pk_in) + 1.0;
+        const int Lo = (r.pk_out != 0.0 ? exp_of(fabs(r.pk_out)) : -1000) + r.ex_out;
+        const int Li = (r.pk_in != 0.0 ? exp_of(fabs(r.pk_in)) : -1000) + r.ex_in;
+        const int po = o.peak_L - Lo, pi = in.peak_L - Li;
+        r.peak_log2 = max(po, pi);
+        r.peak_i = po >= pi ? o.peak_i : in.peak_i;
+    } else {
+        r.sum = sum_fallback;
+    }
+    r.dE = r.gamma * fk * fk / (12.0 * m.a * r.sum);
+    return r;
+}
+
+__device__ __forceinline__ bool cancelled(const DevBatch& b) { return b.cancel && *b.cancel; }
+
+// Safeguarded Cooley-Newton in double-float from the scan bracket.  Every
+// pass updates the count bracket; Newton steps are taken only while the pass
+// sees the level's own node count (so a neighbouring level cannot attract
+// the iteration) and stay inside the bracket, bisection otherwise.  After the
+// match point moves to the peak of |psi| the pass is redone at the same E.
+__global__ void __launch_bounds__(kLongThreads) refine_long_kernel(DevBatch b) {
+    __shared__ LongShared sh;
+    const int n = min(b.hdr->n_long, b.max_levels);
+    for (int q = blockIdx.x; q < n; q += gridDim.x) {
+        const int slot = b.long_list[q];
+        LevelWork w = b.levels[slot];
+        if (w.status & EPSCU_STATUS_NOTFOUND) continue;
+        if (cancelled(b)) {
+            if (threadIdx.x == 0) b.levels[slot].status = w.status | EPSCU_STATUS_CANCELLED;
+            continue;
+        }
+        const PotMeta m = b.meta[w.p];
+        const float2* Wf = b.Wf2 + m.offf;
+        const double* W = b.W64 + m.off;
+        double lo = w.lo, hi = w.hi, E = w.E, sum = 1.0;
+        int k = clamp_k(w, match_index(m, b.Msuf, E));
+        bool done = false, moved_last = false;
+        int it = 0;
+        for (; it < 96; ++it) {
+            const PassDF r = long_pass<1>(m, w, Wf, W, E, k, 1.0, sh);
+            sum = r.sum;
+            if (r.count > w.v) hi = E;
+            else lo = E;
+            if (r.peak_log2 >= 2 && !moved_last) {
+                k = clamp_k(w, r.peak_i);
+                moved_last = true;
+                continue;  // the same energy at the new match point
+            }
+            moved_last = false;
+            const double tol = 1e-12 * fmax(1.0, fabs(E));
+            const double En = E + r.dE;
+            const bool near = r.nodes == w.v || (m.status & EPSCU_STATUS_UNDER);
+            if (near && isfinite(En) && En > lo && En < hi) {
+                E = En;
+                if (fabs(r.dE) <= tol) {
+                    done = true;
+                    break;
+                }
+            } else {
+                E = 0.5 * (lo + hi);
+            }
+            if (hi - lo <= tol) {
+                E = 0.5 * (lo + hi);
+                done = true;
+                break;
+            }
+        }
+        if (threadIdx.x == 0) {
+            if (!done) w.status |= EPSCU_STATUS_MAXITER;
+            w.lo = lo;
+            w.hi = hi;
+            w.E = E;
+            w.k = k;
+            w.norm_k_in = sum;
+            w.iters = it;
+            b.levels[slot] = w;
+        }
+        __syncthreads();
+    }
+}
+
+// The norm pass of a long level and its match-point candidates (as norm_df).
+__global__ void __launch_bounds__(kLongThreads) norm_long_kernel(DevBatch b) {
+    __shared__ LongShared sh;
+    const int n = min(b.hdr->n_long, b.max_levels);
+    for (int q = blockIdx.x; q < n; q += gridDim.x) {
+        const int slot = b.long_list[q];
+        LevelWork w = b.levels[slot];
+        if (w.status & (EPSCU_STATUS_NOTFOUND | EPSCU_STATUS_CANCELLED)) continue;
+        const PotMeta m = b.meta[w.p];
+        const float2* Wf = b.Wf2 + m.offf;
+        const double* W = b.W64 + m.off;
+        int k = w.k;
+        PassDF r = long_pass<1>(m, w, Wf, W, w.E, k, 1.0, sh);
+        if (r.peak_log2 >= 2) {
+            k = clamp_k(w, r.peak_i);
+            r = long_pass<1>(m, w, Wf, W, w.E, k, 1.0, sh);
+        }
+        if (r.nodes != w.v) {
+            const int kt = clamp_k(w, match_index(m, b.Msuf, w.E));
+            PassDF r2 = long_pass<1>(m, w, Wf, W, w.E, kt, 1.0, sh);
+            int k2 = kt;
+            if (r2.nodes != w.v && r2.peak_log2 >= 1) {
+                k2 = clamp_k(w, r2.peak_i);
+                r2 = long_pass<1>(m, w, Wf, W, w.E, k2, 1.0, sh);
+            }
+            if (r2.nodes == w.v) {
+                r = r2;
+                k = k2;
+            }
+        }
+        finalize_df(m, w, r, k);
+        if (threadIdx.x == 0) {
+            if (suspicious(m, w, r.nodes, r.dE) && b.twist_list) {
+                const int t = atomicAdd(&b.hdr->n_twist, 1);
+                if (t < b.max_twist) b.twist_list[t] = slot;
+            }
+            b.levels[slot] = w;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(kLongThreads) write_long_kernel(DevBatch b) {
+    __shared__ LongShared sh;
+    if (!b.psi || b.hdr->error) return;
+    const int n = min(b.hdr->n_long, b.max_levels);
+    for (int q = blockIdx.x; q < n; q += gridDim.x) {
+        const int slot = b.long_list[q];
+        const LevelWork w = b.levels[slot];
+        const PotMeta m = b.meta[w.p];
+        double* out = b.psi + m.psi_off + (int64_t)(w.v - b.min_level) * m.N;
+        const bool none = no_result(w);
+        // zeros outside the window (the whole row without a result), coalesced
+        const int a = none ? m.N : w.j0;
+        for (int i = threadIdx.x; i < a; i += blockDim.x) out[i] = 0.0;
+        if (none) continue;
+        for (int i = w.j1 + 1 + threadIdx.x; i < m.N; i += blockDim.x) out[i] = 0.0;
+        const float2* Wf = b.Wf2 + m.offf;
+        const dfl aE = energy_df(m, w.E);
+        long_side<2>(Wf, aE, w.j0, w.k, +1, out, w.norm_k_out, w.ex_out, sh);
+        long_side<2>(Wf, aE, w.j1, w.k, -1, out, w.norm_k_in, w.ex_in, sh);
+        if (threadIdx.x == 0) out[w.k] = w.ck;
+    }
+}
+
+}  // namespace
+
+void launch_refine_long(const DevBatch& b, int sm_count, cudaStream_t s) {
+    if (!b.long_list) return;
+    refine_long_kernel<<<sm_count * 2, kLongThreads, 0, s>>>(b);
+}
+void launch_norm_long(const DevBatch& b, int sm_count, cudaStream_t s) {
+    if (!b.long_list) return;
+    norm_long_kernel<<<sm_count * 2, kLongThreads, 0, s>>>(b);
+}
+void launch_write_long(const DevBatch& b, int sm_count, cudaStream_t s) {
+    if (!b.long_list) return;
+    write_long_kernel<<<sm_count * 2, kLongThreads, 0, s>>>(b);
+}
+
+}  // namespace epscu

@@ -10,7 +10,7 @@
 // instructions (~1000 FP32-issue equivalents on GB300) for the same pass in
 // native FP64.
 //
-//  newton_df : Cooley corrections from the FP32 energy (1..4 passes) inside an
+//  newton_df : Cooley corrections from the FP32 energy (usually one pass) in an
 //              FP64 count bracket; levels that do not settle go to
 //  fallback_df: multisection on compensated-FP32 counts, one warp per level.
 //  norm_df   : sums, node count, peak of |psi| and the constants of the write.
@@ -21,6 +21,7 @@
 
 #include "common.cuh"
 #include "dfloat.cuh"
+#include "dfpass.cuh"
 #include "launch.h"
 
 namespace epscu {
@@ -28,8 +29,6 @@ namespace epscu {
 namespace {
 
 constexpr int kThreads = 128;
-
-__device__ __forceinline__ int clamp_k(const PotMeta& m, int k) { return max(m.i0 + 1, min(k, m.i1 - 1)); }
 
 // MODE 0: state only (Newton)   MODE 1: + sums, psi-hat, peak   MODE 2: + write
 template <int MODE>
@@ -130,26 +129,15 @@ __device__ __forceinline__ void side_df(const float2* __restrict__ Wf, dfl aE, i
     if (MODE == 1) st.S += f2d(Sacc.h) + f2d(Sacc.l);
 }
 
-__device__ __forceinline__ dfl energy_df(const PotMeta& m, double E) {
-    return df_from_double(__dmul_rn(m.a, E));
-}
-
-struct PassDF {
-    double dE, gamma, sum;
-    double pk_out, pk_in;
-    int ex_out, ex_in;
-    int nodes, count;
-    int peak_i, peak_log2;
-};
-
-// one pass at E with match point k; MODE 0: gamma/count only, MODE 1: + sums
+// one pass at E with match point k over the level's window [w.j0, w.j1];
+// MODE 0: gamma/count only, MODE 1: + sums
 template <int MODE>
-__device__ PassDF pass_df(const PotMeta& m, const float2* __restrict__ Wf, const double* __restrict__ W64, double E,
-                          int k, double sum_fallback) {
+__device__ PassDF pass_df(const PotMeta& m, const LevelWork& w, const float2* __restrict__ Wf,
+                          const double* __restrict__ W64, double E, int k, double sum_fallback) {
     const dfl aE = energy_df(m, E);
     SideDF<MODE> o, in;
-    side_df<MODE>(Wf, aE, m.i0, k, +1, o, nullptr, 0.0, 0);
-    side_df<MODE>(Wf, aE, m.i1, k, -1, in, nullptr, 0.0, 0);
+    side_df<MODE>(Wf, aE, w.j0, k, +1, o, nullptr, 0.0, 0);
+    side_df<MODE>(Wf, aE, w.j1, k, -1, in, nullptr, 0.0, 0);
     const double Tk = __dsub_rn(__dmul_rn(m.a, E), __ldg(W64 + k));
     const double fk = 1.0 + Tk;
     const double Ao = df_to_double(o.A), Do = df_to_double(o.D);
@@ -188,7 +176,7 @@ __global__ void __launch_bounds__(kThreads, 4) newton_df_kernel(DevBatch b) {
         if ((int)(threadIdx.x & 31) >= unit.y) continue;
         const int slot = unit.x + (threadIdx.x & 31);
         LevelWork w = b.levels[slot];
-        if (w.status & (EPSCU_STATUS_NOTFOUND | EPSCU_STATUS_CANCELLED)) continue;
+        if ((w.status & (EPSCU_STATUS_NOTFOUND | EPSCU_STATUS_CANCELLED)) || is_long(w)) continue;
         const PotMeta m = b.meta[w.p];
         const float2* Wf = b.Wf2 + m.offf;
         const double* W = b.W64 + m.off;
@@ -196,12 +184,14 @@ __global__ void __launch_bounds__(kThreads, 4) newton_df_kernel(DevBatch b) {
         double lo = w.lo - 1e-8, hi = w.hi + 1e-8;
         bool ok = false;
         for (int it = 0; it < 4 && !ok; ++it) {
-            const PassDF r = pass_df<0>(m, Wf, W, E, w.k, w.norm_k_in);
+            const PassDF r = pass_df<0>(m, w, Wf, W, E, w.k, w.norm_k_in);
             if (r.count > w.v) hi = fmin(hi, E);
             else lo = fmax(lo, E);
             const double En = E + r.dE;
             if (!isfinite(En) || !(En >= lo && En <= hi) || r.nodes != w.v) break;
-            ok = fabs(r.dE) <= 1e-12 * fmax(1.0, fabs(E));
+            // from the FP32 energy (~1e-9) one step is enough: quadratic
+            // convergence leaves ~1e-13, and norm_df applies one more correction
+            ok = fabs(r.dE) <= (it == 0 ? 1e-8 : 1e-12 * fmax(1.0, fabs(E)));
             E = En;
         }
         if (!ok) {
@@ -238,7 +228,7 @@ __global__ void __launch_bounds__(128) fallback_df_kernel(DevBatch b) {
         {
             // lane 0 checks lo, lane 1 checks hi
             const double Ec = lane == 0 ? lo : hi;
-            const int c = lane < 2 ? pass_df<0>(m, Wf, W, Ec, w.k, 1.0).count : 0;
+            const int c = lane < 2 ? pass_df<0>(m, w, Wf, W, Ec, w.k, 1.0).count : 0;
             const int c_lo = __shfl_sync(0xffffffffu, c, 0), c_hi = __shfl_sync(0xffffffffu, c, 1);
             if (!(c_lo <= w.v && c_hi > w.v)) {
                 lo = fmax(m.e_lo, w.lo0 - m.delta);
@@ -249,7 +239,7 @@ __global__ void __launch_bounds__(128) fallback_df_kernel(DevBatch b) {
             if (hi - lo <= 1e-12 * fmax(1.0, fabs(lo))) break;
             const double step = (hi - lo) / 33.0;
             const double Ej = lo + (lane + 1) * step;
-            const bool above = pass_df<0>(m, Wf, W, Ej, w.k, 1.0).count > w.v;
+            const bool above = pass_df<0>(m, w, Wf, W, Ej, w.k, 1.0).count > w.v;
             const unsigned mask = __ballot_sync(0xffffffffu, above);
             // counts are monotone in E: the first lane above bounds the level
             const int first = mask ? __ffs(mask) - 1 : 32;
@@ -268,35 +258,12 @@ __global__ void __launch_bounds__(128) fallback_df_kernel(DevBatch b) {
     }
 }
 
-// Write the normalisation constants of pass r (match point k) into w.
-__device__ __forceinline__ void finalize_df(const PotMeta& m, LevelWork& w, const PassDF& r, int k) {
-    double ck = 1.0 / sqrt(m.h * r.sum);
-    if (r.pk_out < 0.0) ck = -ck;  // psi > 0 next to the inner wall
-    w.k = k;
-    w.ck = ck;
-    w.norm_k_out = ck / r.pk_out;
-    w.norm_k_in = ck / r.pk_in;
-    w.ex_out = r.ex_out;
-    w.ex_in = r.ex_in;
-    w.dE = r.dE;
-    w.nodes = r.nodes;
-    w.status &= ~EPSCU_STATUS_NOTFOUND;
-    if (!isfinite(r.dE) || !isfinite(ck)) w.status |= EPSCU_STATUS_NONFINITE;
-    if (r.nodes != w.v && !(m.status & EPSCU_STATUS_UNDER)) w.status |= EPSCU_STATUS_NOTFOUND;
-}
-
-// a converged level whose final pass disagrees (node count, or a Cooley
-// correction far above the energy's accuracy) was matched at a poor point
-__device__ __forceinline__ bool suspicious(const PotMeta& m, const LevelWork& w, int nodes, double dE) {
-    return (nodes != w.v && !(m.status & EPSCU_STATUS_UNDER)) || !(fabs(dE) <= 1e-11 * fmax(1.0, fabs(w.E)));
-}
-
 __global__ void __launch_bounds__(kThreads, 4) norm_df_kernel(DevBatch b) {
     for (int2 unit; next_unit(b, kQNormDF, unit);) {
         if ((int)(threadIdx.x & 31) >= unit.y) continue;
         const int slot = unit.x + (threadIdx.x & 31);
         LevelWork w = b.levels[slot];
-        if (w.status & (EPSCU_STATUS_NOTFOUND | EPSCU_STATUS_CANCELLED)) continue;
+        if ((w.status & (EPSCU_STATUS_NOTFOUND | EPSCU_STATUS_CANCELLED)) || is_long(w)) continue;
         const PotMeta m = b.meta[w.p];
         const float2* Wf = b.Wf2 + m.offf;
         const double* W = b.W64 + m.off;
@@ -304,18 +271,18 @@ __global__ void __launch_bounds__(kThreads, 4) norm_df_kernel(DevBatch b) {
         // pass, the outer turning point and its peak; the first whose
         // stitched solution has v nodes wins
         int k = w.k;
-        PassDF r = pass_df<1>(m, Wf, W, w.E, k, 1.0);
-        if (r.peak_log2 >= 1) {
-            k = clamp_k(m, r.peak_i);
-            r = pass_df<1>(m, Wf, W, w.E, k, 1.0);
+        PassDF r = pass_df<1>(m, w, Wf, W, w.E, k, 1.0);
+        if (r.peak_log2 >= 2) {
+            k = clamp_k(w, r.peak_i);
+            r = pass_df<1>(m, w, Wf, W, w.E, k, 1.0);
         }
         if (r.nodes != w.v) {
-            const int kt = clamp_k(m, match_index(m, b.Msuf, w.E));
-            PassDF r2 = pass_df<1>(m, Wf, W, w.E, kt, 1.0);
+            const int kt = clamp_k(w, match_index(m, b.Msuf, w.E));
+            PassDF r2 = pass_df<1>(m, w, Wf, W, w.E, kt, 1.0);
             int k2 = kt;
             if (r2.nodes != w.v && r2.peak_log2 >= 1) {
-                k2 = clamp_k(m, r2.peak_i);
-                r2 = pass_df<1>(m, Wf, W, w.E, k2, 1.0);
+                k2 = clamp_k(w, r2.peak_i);
+                r2 = pass_df<1>(m, w, Wf, W, w.E, k2, 1.0);
             }
             if (r2.nodes == w.v) {
                 r = r2;
@@ -335,8 +302,8 @@ __global__ void __launch_bounds__(kThreads, 4) norm_df_kernel(DevBatch b) {
 // samples u_{k-1}/u_k every kTwistSample points, one full inward sweep forms
 // gamma_k at the same points, and the match point becomes argmin |gamma_k|
 // (at an eigenvalue |gamma_k| is smallest where the eigenvector is largest;
-// the rule of Dhillon and Parlett's twisted factorisations).  Then the norm
-// pass is redone there.
+// the rule of Dhillon and Parlett's twisted factorisations).  Then Newton
+// and the norm pass are redone there.
 __global__ void __launch_bounds__(64) twist_df_kernel(DevBatch b) {
     const int n = min(b.hdr->n_twist, b.max_twist);
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
@@ -350,16 +317,16 @@ __global__ void __launch_bounds__(64) twist_df_kernel(DevBatch b) {
         const double aEd = __dmul_rn(m.a, w.E);
         // outward: before point i the state is ~ (u_i, u_i - u_{i-1})
         dfl A = {1.0f, 0.0f}, D = {1.0f, 0.0f};
-        for (int i = m.i0; i < m.i1; ++i) {
-            const int j = (i - m.i0) / kTwistSample;
-            if ((i - m.i0) % kTwistSample == 0 && j < b.twist_stride) rho[j] = df_to_double(D) / df_to_double(A);
+        for (int i = w.j0; i < w.j1; ++i) {
+            const int j = (i - w.j0) / kTwistSample;
+            if ((i - w.j0) % kTwistSample == 0 && j < b.twist_stride) rho[j] = df_to_double(D) / df_to_double(A);
             const float2 wv = __ldg(Wf + i);
             dfl T = two_sum(aE.h, -wv.x);
             T = fast_two_sum(T.h, __fadd_rn(T.l, __fsub_rn(aE.l, wv.y)));
             const dfl X = df_add(D, df_mulf(A, -12.0f));
             D = df_add(D, df_mul(T, X));
             A = df_add(A, df_add(df_mul(T, A), D));
-            if (((i - m.i0) & 7) == 7) {
+            if (((i - w.j0) & 7) == 7) {
                 const float mm = fmaxf(fabsf(A.h), fabsf(D.h));
                 if (mm > 0.0f && mm < INFINITY) {
                     const float sc = fpow2(-max(-120, min(120, fexp(mm))));
@@ -372,9 +339,9 @@ __global__ void __launch_bounds__(64) twist_df_kernel(DevBatch b) {
         dfl C = {1.0f, 0.0f}, E = {1.0f, 0.0f};
         double best = INFINITY;
         int kbest = w.k;
-        for (int i = m.i1; i > m.i0; --i) {
-            if ((i - m.i0) % kTwistSample == 0 && i <= m.i1 - 1) {
-                const int j = (i - m.i0) / kTwistSample;
+        for (int i = w.j1; i > w.j0; --i) {
+            if ((i - w.j0) % kTwistSample == 0 && i <= w.j1 - 1) {
+                const int j = (i - w.j0) / kTwistSample;
                 if (j < b.twist_stride) {
                     const double Ti = aEd - __ldg(W + i);
                     const double gam = -12.0 * Ti / (1.0 + Ti) + rho[j] + df_to_double(E) / df_to_double(C);
@@ -390,7 +357,7 @@ __global__ void __launch_bounds__(64) twist_df_kernel(DevBatch b) {
             const dfl X = df_add(E, df_mulf(C, -12.0f));
             E = df_add(E, df_mul(T, X));
             C = df_add(C, df_add(df_mul(T, C), E));
-            if (((m.i1 - i) & 7) == 7) {
+            if (((w.j1 - i) & 7) == 7) {
                 const float mm = fmaxf(fabsf(C.h), fabsf(E.h));
                 if (mm > 0.0f && mm < INFINITY) {
                     const float sc = fpow2(-max(-120, min(120, fexp(mm))));
@@ -399,8 +366,18 @@ __global__ void __launch_bounds__(64) twist_df_kernel(DevBatch b) {
                 }
             }
         }
-        const int k = clamp_k(m, kbest);
-        const PassDF r = pass_df<1>(m, Wf, W, w.E, k, 1.0);
+        const int k = clamp_k(w, kbest);
+        // Newton at the new match point: the energy was settled at the old one,
+        // so its Cooley correction here may still be above the tolerance
+        double E1 = w.E;
+        PassDF r = pass_df<1>(m, w, Wf, W, E1, k, 1.0);
+        for (int it = 0; it < 8; ++it) {
+            if (r.nodes != w.v || !isfinite(r.dE) || !(fabs(r.dE) < 1e-7)) break;
+            if (fabs(r.dE) <= 1e-12 * fmax(1.0, fabs(E1))) break;
+            E1 += r.dE;
+            r = pass_df<1>(m, w, Wf, W, E1, k, 1.0);
+        }
+        w.E = E1;
         finalize_df(m, w, r, k);
         b.levels[slot] = w;
     }
@@ -408,23 +385,32 @@ __global__ void __launch_bounds__(64) twist_df_kernel(DevBatch b) {
 
 __global__ void __launch_bounds__(kThreads, 4) write_df_kernel(DevBatch b) {
     if (!b.psi || b.hdr->error) return;
+    const int lane = threadIdx.x & 31;
     for (int2 unit; next_unit(b, kQWriteDF, unit);) {
-        if ((int)(threadIdx.x & 31) >= unit.y) continue;
-        const int slot = unit.x + (threadIdx.x & 31);
+        // zeros outside each level's window (the whole row of a level without a
+        // result), stored by the whole warp with coalesced stores
+        for (int u = 0; u < unit.y; ++u) {
+            const LevelWork wu = b.levels[unit.x + u];
+            if (is_long(wu)) continue;  // written by write_long
+            const int N = b.meta[wu.p].N;
+            double* row = b.psi + b.meta[wu.p].psi_off + (int64_t)(wu.v - b.min_level) * N;
+            const bool none = no_result(wu);
+            const int a = none ? N : wu.j0;
+            for (int i = lane; i < a; i += 32) row[i] = 0.0;
+            if (!none)
+                for (int i = wu.j1 + 1 + lane; i < N; i += 32) row[i] = 0.0;
+        }
+        if (lane >= unit.y) continue;
+        const int slot = unit.x + lane;
         const LevelWork w = b.levels[slot];
+        if (no_result(w) || is_long(w)) continue;
         const PotMeta m = b.meta[w.p];
         double* out = b.psi + m.psi_off + (int64_t)(w.v - b.min_level) * m.N;
-        for (int i = 0; i < m.i0; ++i) out[i] = 0.0;
-        for (int i = m.i1 + 1; i < m.N; ++i) out[i] = 0.0;
-        if (w.status & (EPSCU_STATUS_NOTFOUND | EPSCU_STATUS_CANCELLED | EPSCU_STATUS_NONFINITE)) {
-            for (int i = m.i0; i <= m.i1; ++i) out[i] = 0.0;
-            continue;
-        }
         const float2* Wf = b.Wf2 + m.offf;
         const dfl aE = energy_df(m, w.E);
         SideDF<2> st;
-        side_df<2>(Wf, aE, m.i0, w.k, +1, st, out, w.norm_k_out, w.ex_out);
-        side_df<2>(Wf, aE, m.i1, w.k, -1, st, out, w.norm_k_in, w.ex_in);
+        side_df<2>(Wf, aE, w.j0, w.k, +1, st, out, w.norm_k_out, w.ex_out);
+        side_df<2>(Wf, aE, w.j1, w.k, -1, st, out, w.norm_k_in, w.ex_in);
         out[w.k] = w.ck;
     }
 }

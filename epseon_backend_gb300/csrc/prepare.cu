@@ -8,6 +8,7 @@
 #include <math.h>
 
 #include "common.cuh"
+#include "dfpass.cuh"
 #include "launch.h"
 
 namespace epscu {
@@ -288,7 +289,54 @@ __global__ void bracket_kernel(DevBatch b) {
         }
         w.lo0 = w.lo;
         w.hi0 = w.hi;
+        w.j0 = m.i0;
+        w.j1 = m.i1;
+        w.pad0 = w.pad1 = 0;
         b.levels[m.level_base + s] = w;
+    }
+}
+
+// Decay window of every level slot (fast method), at E_up = hi0 + 2 delta:
+// an energy above every energy the level's passes use (bracket, Newton steps,
+// the fallback's widened bracket), so one window serves all of them.  Levels
+// whose window is longer than kLongWindow go to the long list (CTA-per-level
+// passes).  One warp per level.
+__global__ void __launch_bounds__(128) window_kernel(DevBatch b) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int n_warps = (gridDim.x * blockDim.x) >> 5;
+    const int total = b.hdr->total_levels;
+    for (int slot = warp; slot < total; slot += n_warps) {
+        const LevelWork w = b.levels[slot];
+        if (w.status & EPSCU_STATUS_NOTFOUND) continue;
+        const PotMeta m = b.meta[w.p];
+        const int2 jw = decay_window(m, b.W64 + m.off, b.Msuf, w.hi0 + 2.0 * m.delta, kWindowDecay);
+        if ((threadIdx.x & 31) == 0) {
+            b.levels[slot].j0 = jw.x;
+            b.levels[slot].j1 = jw.y;
+            if (jw.y - jw.x > kLongWindow && b.long_list) {
+                const int q = atomicAdd(&b.hdr->n_long, 1);
+                if (q < b.max_levels) b.long_list[q] = slot;
+            }
+        }
+    }
+}
+
+// Decay windows of the scan: entry (p, q) is the window of the highest trial
+// energy of block q (kScanWinBlock consecutive trial energies) of potential p,
+// which contains the windows of every energy of the block.  One warp per entry.
+__global__ void __launch_bounds__(128) scan_window_kernel(DevBatch b, int n_blk) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int n_warps = (gridDim.x * blockDim.x) >> 5;
+    const int total = b.n * n_blk;
+    for (int e = warp; e < total; e += n_warps) {
+        const int p = e / n_blk, q = e % n_blk;
+        const PotMeta m = b.meta[p];
+        int2 jw = make_int2(m.i0, m.i1);
+        if (!(m.status & EPSCU_STATUS_BAD)) {
+            const int j = min((q + 1) * kScanWinBlock, b.n_trial) - 1;
+            jw = decay_window(m, b.W64 + m.off, b.Msuf, trial_energy(m, j), kWindowDecay);
+        }
+        if ((threadIdx.x & 31) == 0) b.scan_win[e] = jw;
     }
 }
 
@@ -376,6 +424,15 @@ void launch_level_setup(const DevBatch& b, cudaStream_t s) {
     level_setup_kernel<<<1, 1024, 0, s>>>(b);
     unit_setup_kernel<<<1, 1024, 0, s>>>(b);
     bracket_kernel<<<b.n, 128, 0, s>>>(b);
+}
+
+void launch_window(const DevBatch& b, int sm_count, cudaStream_t s) {
+    window_kernel<<<sm_count * 8, 128, 0, s>>>(b);
+}
+
+void launch_scan_window(const DevBatch& b, int sm_count, cudaStream_t s) {
+    if (!b.scan_win) return;
+    scan_window_kernel<<<sm_count * 8, 128, 0, s>>>(b, (b.n_trial + kScanWinBlock - 1) / kScanWinBlock);
 }
 
 void launch_tabulate(int32_t n, const int32_t* kind, const double* params, const int64_t* offsets, const int32_t* N,

@@ -87,26 +87,25 @@ __device__ __forceinline__ void fence_barrier_init() {
 
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-// Tile t of the item's sequence: outward tiles ascending over [i0, k-1], then
-// inward tiles descending over [k+1, i1].
+// Tile t of the item's sequence: outward tiles ascending over [j0, k-1], then
+// inward tiles descending over [k+1, j1] ([j0, j1] = the item's window).
 struct TileSeq {
     int out_first, n_out, in_first, n_in;  // tile indices
     __device__ int tile(int t) const { return t < n_out ? out_first + t : in_first - (t - n_out); }
     __device__ int size() const { return n_out + n_in; }
 };
 
-__device__ __forceinline__ TileSeq make_seq(const PotMeta& m, int tile) {
+__device__ __forceinline__ TileSeq make_seq(int j0, int j1, int k, int tile) {
     TileSeq s;
-    const int k = m.k_scan;
-    if (k > m.i0) {
-        s.out_first = m.i0 / tile;
+    if (k > j0) {
+        s.out_first = j0 / tile;
         s.n_out = (k - 1) / tile - s.out_first + 1;
     } else {
         s.out_first = 0;
         s.n_out = 0;
     }
-    if (k < m.i1) {
-        s.in_first = m.i1 / tile;
+    if (k < j1) {
+        s.in_first = j1 / tile;
         s.n_in = s.in_first - (k + 1) / tile + 1;
     } else {
         s.in_first = 0;
@@ -236,7 +235,28 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
             if (j < b.n_trial) b.counts[(int64_t)p * b.n_trial + j] = 0;
             continue;  // uniform across the CTA
         }
-        const TileSeq seq = make_seq(m, TILE);
+        // the item's window: union of the decay windows of its energy blocks
+        // (they contain the twist index k_scan = argmin V), else [i0, i1]
+        int j0 = m.i0, j1 = m.i1;
+        if (b.scan_win) {
+            const int nb = (b.n_trial + kScanWinBlock - 1) / kScanWinBlock;
+            const int e0 = (item % ipp) * THREADS;
+            const int q0 = e0 / kScanWinBlock, q1 = min(nb - 1, (e0 + THREADS - 1) / kScanWinBlock);
+            j0 = m.i1;
+            j1 = m.i0;
+            for (int q = q0; q <= q1; ++q) {
+                const int2 wq = b.scan_win[(int64_t)p * nb + q];
+                j0 = min(j0, wq.x);
+                j1 = max(j1, wq.y);
+            }
+            j0 = min(j0, m.k_scan);
+            j1 = max(j1, m.k_scan);
+        }
+        const TileSeq seq = make_seq(j0, j1, m.k_scan, TILE);
+        if (tid == 0) {
+            const int n_e = min(THREADS, b.n_trial - (item % ipp) * THREADS);
+            atomicAdd(&b.hdr->scan_updates, (unsigned long long)n_e * (unsigned long long)(j1 - j0));
+        }
         const int L = seq.size();
         const float2* src = b.Wf2 + m.offf;
 
@@ -256,7 +276,7 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
         const float aEh = __double2float_rn(aE);
         const float aEl = __double2float_rn(aE - (double)aEh);
         const int k = m.k_scan;
-        float A = 1.0f, D = 1.0f;  // u_{i0} = 1, u_{i0-1} = 0
+        float A = 1.0f, D = 1.0f;  // u_{j0} = 1, u_{j0-1} = 0
         float Ao = 1.0f, Do = 1.0f;
         int nodes = 0;
         bool inward = false;
@@ -271,17 +291,17 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
             const float2* tb = buf + st * TILE;
             const int T0 = seq.tile(t) * TILE;
             if (t < seq.n_out) {
-                const int a0 = max(m.i0, T0), a1 = min(k - 1, T0 + TILE - 1);
+                const int a0 = max(j0, T0), a1 = min(k - 1, T0 + TILE - 1);
                 run_up(tb, T0, a0, a1, aEh, aEl, A, D, nodes);
             } else {
                 if (!inward) {
                     inward = true;
                     Ao = A;
                     Do = D;
-                    A = 1.0f;  // v_{i1} = 1, v_{i1+1} = 0
+                    A = 1.0f;  // v_{j1} = 1, v_{j1+1} = 0
                     D = 1.0f;
                 }
-                const int a0 = min(m.i1, T0 + TILE - 1), a1 = max(k + 1, T0);
+                const int a0 = min(j1, T0 + TILE - 1), a1 = max(k + 1, T0);
                 run_down(tb, T0, a0, a1, aEh, aEl, A, D, nodes);
             }
             __syncthreads();  // every thread is done with stage st
@@ -299,7 +319,7 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
         }
         if (s_abort) break;
         g_tile += L;
-        if (!inward) {  // no inward tiles: k == i1
+        if (!inward) {  // no inward tiles: k == j1
             Ao = A;
             Do = D;
             A = 1.0f;

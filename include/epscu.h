@@ -204,7 +204,7 @@ epscu_status epscu_cancel(epscu_ctx* ctx);
  * stream) and the counters the roofline uses. */
 typedef struct epscu_stats {
     float ms_prepare, ms_scan, ms_refine32, ms_polish64, ms_write, ms_total;
-    int64_t scan_point_updates;    /* trial energies x interior points */
+    int64_t scan_point_updates;    /* trial energies x points of the scan (its window for the fast method) */
     int64_t refine_point_updates;  /* FP32 refinement passes x points */
     int64_t fp64_point_updates;    /* FP64 passes x points */
     int64_t psi_bytes;             /* wavefunction bytes written */

@@ -175,12 +175,14 @@ def test_bump_wavefunctions_all_levels(ctx, method):
 
 @pytest.mark.parametrize("method", [capi.METHOD_PLAIN_FP64, capi.METHOD_FAST_FP32C])
 def test_long_grid_top_levels(ctx, method):
-    """Long grid (one heavy Morse, N = 2^20, ~280 bound levels): the ten highest
-    levels (and the lowest three) against the oracle, with a reduced number of
-    trial energies so the oracle finishes in seconds."""
+    """Long grid (one heavy Morse, N = 2^20, ~280 bound levels): the lowest three
+    levels (windows of ~4e4 points: one lane per level), a middle band and the
+    ten highest (windows of 9e4 - 6.5e5 points: the fast method's CTA-per-level
+    passes) against the oracle, with a reduced number of trial energies so the
+    oracle finishes in seconds."""
     b = synth.morse_long(n_trial=4096)
     V = b.V(0)
-    for lo, hi in ((0, 2), (270, 279)):
+    for lo, hi in ((0, 2), (100, 104), (270, 279)):
         ref = O.solve_batch([V], b.r_min, b.r_max, b.mu, b.e_cap, b.n_trial, min_level=lo, max_level=hi,
                             want_psi=True)[0]
         assert ref.n_total == 280
