@@ -39,6 +39,9 @@ METRIC = "bound levels/s at |dE|<=1e-9 Eh vs FP64 oracle; batched+adjoint vs pla
 UNIT = "levels/s"
 E_TOL = 1e-9
 CPU_SAMPLE = 96  # potentials of the workload the CPU legs time
+# dram__bytes_read.sum + dram__bytes_write.sum of one scan32 launch per grid
+# point, ncu on the 128-potential mixed batch (18.12 MB / 2,242,300 points)
+SCAN32_DRAM_BYTES_PER_POINT = 8.08
 
 
 def dist_env():
@@ -385,10 +388,23 @@ def main():
     # compensation, renormalisation and sign bookkeeping are not counted.
     scan_flops = 9.0 * st.scan_point_updates
     ach = scan_flops / (st.ms_scan * 1e-3) / 1e12
+    # DRAM bytes per launch: ncu measured SCAN32_DRAM_BYTES_PER_POINT on the
+    # 128-potential mixed batch (the potential read once; tiles re-read from
+    # L2 and shared memory), scaled by the grid points of this workload
+    traffic = SCAN32_DRAM_BYTES_PER_POINT * float(b.N.sum())
     roof = {"bound": "fp32_alu", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s", "frac": ach / fp32_peak,
-            "traffic": None, "kernel": "scan32_kernel",
+            "traffic": traffic, "traffic_unit": "bytes per launch (ncu-measured per-point DRAM bytes x points)",
+            "kernel": "scan32_kernel",
             "algorithmic": {"point_updates": int(st.scan_point_updates), "flops_per_update": 9},
             "peak_source": "measured FP32 FMA burst (epscu_measure_fma_peaks), 2 flops per FMA"}
+    # the per-level stages in the same unit (algorithmic point-updates counted
+    # by the kernels over the level windows; latency-bound lane marches)
+    stage_rates = {
+        "refine32_point_updates_per_s": st.refine_point_updates / (st.ms_refine32 * 1e-3) if st.ms_refine32 > 0 else None,
+        "double_float_point_updates_per_s": st.fp64_point_updates / (st.ms_polish64 * 1e-3) if st.ms_polish64 > 0 else None,
+        "refine32_point_updates": int(st.refine_point_updates),
+        "double_float_point_updates": int(st.fp64_point_updates),
+    }
     # the FP64-pipe view of the plain solver's dominant kernel, for comparison
     roof_plain = {"kernel": "scan64_kernel", "achieved": 9.0 * plain_stats.scan_point_updates
                   / (plain_stats.ms_scan * 1e-3) / 1e12, "peak": fp64_peak, "unit": "TFLOP/s"}
@@ -429,9 +445,11 @@ def main():
         "speedup_vs_plain_fp64": value / plain_value,
         "stages_ms": {"prepare": st.ms_prepare, "scan32": st.ms_scan, "refine32": st.ms_refine32,
                       "polish64": st.ms_polish64, "write64": st.ms_write, "solve_total": st.ms_total,
-                      "fallbacks": st.fallbacks, "twist_searches": st.twist_searches},
+                      "fallbacks": st.fallbacks, "twist_searches": st.twist_searches,
+                      "norm_redos": st.norm_redos},
         "roofline": roof,
         "roofline_plain_fp64": roof_plain,
+        "stage_rates": stage_rates,
         "psi_write": {"bytes": st.psi_bytes, "GB_per_s": write_gbs, "hbm_peak_GBs": hbm},
         "e2e": {"value": e2e_good * world / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,

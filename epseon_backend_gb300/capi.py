@@ -108,7 +108,7 @@ class Stats(C.Structure):
         ("kernel_launches", C.c_int32),
         ("fallbacks", C.c_int32),
         ("twist_searches", C.c_int32),
-        ("reserved", C.c_int32),
+        ("norm_redos", C.c_int32),
     ]
 
 

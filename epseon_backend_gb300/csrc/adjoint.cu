@@ -6,7 +6,10 @@
 // sum psi^2 h = 1, so for L(E) the gradient is
 //     dL/dV_i = sum_v dL/dE_v psi_v(r_i)^2 h.
 // One thread per grid point, reading the potential's psi rows coalesced; the
-// kernel is HBM-bound (8 bytes of psi per level and point).
+// kernel is HBM-bound (8 bytes of psi per level and point).  psi is zero
+// outside each level's window [j0, j1] (the written rows hold zeros there), so
+// those reads are skipped: on the mixed batch the fast method's windows hold
+// about a fifth of the row points.
 #include <cuda_runtime.h>
 
 #include "common.cuh"
@@ -26,17 +29,21 @@ __global__ void adjoint_kernel(DevBatch b, const double* __restrict__ gE, double
     if (i >= m.N) return;
     const double* rows = psi + m.psi_off + i;
     const double* g = gE + (int64_t)p * b.level_capacity;
+    const LevelWork* lw = b.levels + m.level_base;
     double acc = 0.0;
     int s = 0;
     for (; s + 4 <= m.n_out; s += 4) {
-        const double p0 = __ldg(rows + (int64_t)s * m.N), p1 = __ldg(rows + (int64_t)(s + 1) * m.N);
-        const double p2 = __ldg(rows + (int64_t)(s + 2) * m.N), p3 = __ldg(rows + (int64_t)(s + 3) * m.N);
-        acc = fma(g[s] * p0, p0, acc);
-        acc = fma(g[s + 1] * p1, p1, acc);
-        acc = fma(g[s + 2] * p2, p2, acc);
-        acc = fma(g[s + 3] * p3, p3, acc);
+        double v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int2 jw = make_int2(lw[s + u].j0, lw[s + u].j1);
+            v[u] = (i >= jw.x && i <= jw.y) ? __ldg(rows + (int64_t)(s + u) * m.N) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) acc = fma(g[s + u] * v[u], v[u], acc);
     }
     for (; s < m.n_out; ++s) {
+        if (i < lw[s].j0 || i > lw[s].j1) continue;
         const double v = __ldg(rows + (int64_t)s * m.N);
         acc = fma(g[s] * v, v, acc);
     }

@@ -72,15 +72,21 @@ struct Header {
     int32_t n_twist;        // levels handed to the twist-index search
     int32_t queue[8];       // work-queue heads of the per-level kernels
     int32_t n_long;         // levels whose window takes the CTA-per-level passes
-    int32_t pad;
-    unsigned long long scan_updates;  // point-updates the windowed FP32 scan performed
+    int32_t n_redo;         // norm passes redone at E + dE
+    unsigned long long scan_updates;    // point-updates the windowed FP32 scan performed
+    unsigned long long refine_updates;  // point-updates of the FP32 refinement passes
+    unsigned long long df_updates;      // point-updates of the double-float passes
 };
 
 // queue ids of the per-level kernels
 enum { kQRefine32 = 0, kQNewtonDF, kQNormDF, kQWriteDF, kQBisect64, kQNorm64, kQWrite64 };
 
-// internal level flag: the Newton stage handed the level to the bisection fallback
+// internal level flags (not reported: gather keeps the public bits only)
+// the Newton stage handed the level to the fallback
 #define EPSCU_STATUS_FALLBACK 0x10000
+// the level's passes run one CTA per level (longwin.cu)
+#define EPSCU_STATUS_LONG 0x20000
+#define EPSCU_STATUS_PUBLIC 0xffff
 // spacing of the samples of the twist-index search
 constexpr int kTwistSample = 64;
 
@@ -137,73 +143,6 @@ __device__ __forceinline__ int match_index(const PotMeta& m, const double* __res
         else hi = mid - 1;
     }
     return lo;
-}
-
-// Decay window at energy Eu (fast method only; one call per warp, all lanes).
-// Beyond the classical turning points of Eu (V > Eu there) the discrete
-// solution decays at least by the constant-coefficient rate of the Numerov
-// recurrence, acosh(1 + 6 t_i) per step with t_i = W_i - a Eu (for small t it
-// is kappa h, the WKB exponent).  The window ends where that exponent, summed
-// from the turning point, reaches `decay`: Dirichlet ends there change the
-// solution by about e^-decay relative to its size at the turning point and an
-// eigenvalue by a relative e^-2 decay, and every energy below Eu has a
-// narrower window.  Classical choice of the starting point of the inward
-// integration in Numerov-Cooley codes.  Returns [j0, j1] within [i0, i1].
-__device__ __forceinline__ int2 decay_window(const PotMeta& m, const double* __restrict__ W,
-                                             const double* __restrict__ Msuf, double Eu, float decay) {
-    const int lane = threadIdx.x & 31;
-    const unsigned full = 0xffffffffu;
-    const double aEu = m.a * Eu;
-    // outer side: the last allowed point (V_i <= Eu), then outward
-    const int t_out = match_index(m, Msuf, Eu);
-    int j1 = m.i1;
-    float X = 0.0f;
-    for (int base = t_out + 1; base <= m.i1; base += 32) {
-        const int i = base + lane;
-        float s = 0.0f;
-        if (i <= m.i1) s = acoshf(1.0f + 6.0f * fmaxf((float)(W[i] - aEu), 0.0f));
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const float y = __shfl_up_sync(full, s, o);
-            if (lane >= o) s += y;
-        }
-        const unsigned hit = __ballot_sync(full, i <= m.i1 && X + s >= decay);
-        if (hit) {
-            j1 = base + __ffs(hit) - 1;
-            break;
-        }
-        X += __shfl_sync(full, s, 31);
-    }
-    // inner side: the first allowed point, then inward
-    int t_in = m.i1;
-    for (int base = m.i0; base <= m.i1; base += 32) {
-        const int i = base + lane;
-        const unsigned hit = __ballot_sync(full, i <= m.i1 && W[i] <= aEu);
-        if (hit) {
-            t_in = base + __ffs(hit) - 1;
-            break;
-        }
-    }
-    int j0 = m.i0;
-    X = 0.0f;
-    for (int base = t_in - 1; base >= m.i0; base -= 32) {
-        const int i = base - lane;
-        float s = 0.0f;
-        if (i >= m.i0) s = acoshf(1.0f + 6.0f * fmaxf((float)(W[i] - aEu), 0.0f));
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const float y = __shfl_up_sync(full, s, o);
-            if (lane >= o) s += y;
-        }
-        const unsigned hit = __ballot_sync(full, i >= m.i0 && X + s >= decay);
-        if (hit) {
-            j0 = base - (__ffs(hit) - 1);
-            break;
-        }
-        X += __shfl_sync(full, s, 31);
-    }
-    if (j1 - j0 < 4) return make_int2(m.i0, m.i1);
-    return make_int2(j0, j1);
 }
 
 // e-folds of decay at the ends of the fast method's windows

@@ -9,11 +9,15 @@
 
 namespace epscu {
 
-// Windows longer than this many points take the CTA-per-level passes of
-// longwin.cu (parallel prefix over chunks) instead of one lane per level.
+// Windows longer than kLongWindow points take the CTA-per-level passes of
+// longwin.cu (parallel prefix over chunks) instead of one lane per level; so
+// do windows longer than kFewWindow points when the batch has at most
+// kFewLevelsPerSM levels per SM (too few lanes to fill the GPU).
 constexpr int kLongWindow = 65536;
+constexpr int kFewWindow = 4096;
+constexpr int kFewLevelsPerSM = 4;
 
-__device__ __forceinline__ bool is_long(const LevelWork& w) { return w.j1 - w.j0 > kLongWindow; }
+__device__ __forceinline__ bool is_long(const LevelWork& w) { return (w.status & EPSCU_STATUS_LONG) != 0; }
 
 // match points stay inside the level's window, off its two end points
 __device__ __forceinline__ int clamp_k(const LevelWork& w, int k) { return max(w.j0 + 1, min(k, w.j1 - 1)); }
@@ -51,6 +55,13 @@ __device__ __forceinline__ void finalize_df(const PotMeta& m, LevelWork& w, cons
 // correction far above the energy's accuracy) was matched at a poor point
 __device__ __forceinline__ bool suspicious(const PotMeta& m, const LevelWork& w, int nodes, double dE) {
     return (nodes != w.v && !(m.status & EPSCU_STATUS_UNDER)) || !(fabs(dE) <= 1e-11 * fmax(1.0, fabs(w.E)));
+}
+
+// psi is only as accurate as the energy it is computed at (error ~ |E - E_v|
+// over the gap to the next level, 1e-5 Eh near dissociation): a norm pass
+// whose Cooley correction is above this is redone once at E + dE
+__device__ __forceinline__ bool redo_norm(const LevelWork& w, const PassDF& r) {
+    return r.nodes == w.v && isfinite(r.dE) && fabs(r.dE) > 1e-13 * fmax(1.0, fabs(w.E)) && fabs(r.dE) < 1e-8;
 }
 
 __device__ __forceinline__ bool no_result(const LevelWork& w) {

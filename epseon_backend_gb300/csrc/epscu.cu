@@ -285,13 +285,10 @@ void enqueue_pipeline(epscu_ctx* ctx, const DevBatch& b, int method, bool want_p
     };
     rec(0);
     launch_prepare(b, s);
+    if (method == EPSCU_METHOD_FAST_FP32C) launch_scan_window(b, ctx->sm_count, s);  // timed with prepare
     rec(1);
-    if (method == EPSCU_METHOD_PLAIN_FP64) {
-        launch_scan64(b, s);
-    } else {
-        launch_scan_window(b, ctx->sm_count, s);
-        launch_scan32(b, shape, ctx->sm_count, s);
-    }
+    if (method == EPSCU_METHOD_PLAIN_FP64) launch_scan64(b, s);
+    else launch_scan32(b, shape, ctx->sm_count, s);
     rec(2);
     launch_level_setup(b, s);
     if (method == EPSCU_METHOD_PLAIN_FP64) {
@@ -307,13 +304,13 @@ void enqueue_pipeline(epscu_ctx* ctx, const DevBatch& b, int method, bool want_p
         launch_refine_long(b, ctx->sm_count, s);
         rec(3);
         launch_newton_df(b, ctx->sm_count, s);
-        launch_fallback_df(b, ctx->sm_count, s);
+        launch_fallback_long(b, ctx->sm_count, s);
         launch_norm_df(b, ctx->sm_count, s);
         launch_norm_long(b, ctx->sm_count, s);
         launch_twist_df(b, ctx->sm_count, s);
         rec(4);
         if (want_psi) {
-            launch_write_df(b, ctx->sm_count, s);
+            launch_scale_psi(b, ctx->sm_count, s);  // rows written unnormalised by norm_df / twist_df
             launch_write_long(b, ctx->sm_count, s);
         }
     }
@@ -415,7 +412,12 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     b.order = (int32_t*)ctx->get("order", sizeof(int32_t) * n, &ce);
     b.scan_win = nullptr;
     b.long_list = nullptr;
+    b.Mpre = nullptr;
+    b.Bmin = nullptr;
     if (method == EPSCU_METHOD_FAST_FP32C) {
+        b.Mpre = (double*)ctx->get("Mpre", sizeof(double) * total_points, &ce);
+        b.Bmin = (float*)ctx->get("Bmin", sizeof(float) * (size_t)(total_padded / 32 + 1), &ce);
+        if (!b.Mpre || !b.Bmin) return fail(EPSCU_ERR_NOMEM, "device arena (window bounds)");
         b.long_list = (int32_t*)ctx->get("long_list", sizeof(int32_t) * lv, &ce);
         if (!b.long_list) return fail(EPSCU_ERR_NOMEM, "device arena (long list)");
         const size_t nb = (size_t)(batch->n_trial + kScanWinBlock - 1) / kScanWinBlock;
@@ -634,16 +636,24 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     st.n_levels = nlev;
     st.fallbacks = hh->fallbacks;
     st.twist_searches = hh->n_twist;
+    st.norm_redos = hh->n_redo;
     st.psi_bytes = want_psi ? psi_total * 8 : 0;
-    st.kernel_launches = 9 + (want_psi ? 1 : 0) + (method == EPSCU_METHOD_FAST_FP32C ? 2 : 0);
+    // plain: prepare, scan64, level/unit setup, bracket, bisect64, norm64,
+    // twist64, gather (+ write64); fast: prepare, scan window, scan32, level/unit
+    // setup, bracket, window, refine32, refine_long, newton_df, fallback
+    // (refine_long over the fallback list), norm_df, norm_long, twist_df,
+    // gather (+ scale_psi, write_long)
+    st.kernel_launches = method == EPSCU_METHOD_FAST_FP32C ? 16 + (want_psi ? 2 : 0) : 9 + (want_psi ? 1 : 0);
     if (method == EPSCU_METHOD_PLAIN_FP64) {
         st.refine_point_updates = 0;
         int64_t bis = 0;
         for (int p = 0; p < n; ++p) bis += (int64_t)std::max(0, hm[p].i1 - hm[p].i0) * hm[p].n_out * hm[p].n_bisect;
         st.fp64_point_updates = scan_pts + bis + lvl_pts * (want_psi ? 2 : 1);
     } else {
-        st.refine_point_updates = -1;  // data-dependent iteration counts
-        st.fp64_point_updates = lvl_pts * (want_psi ? 3 : 2);
+        // counted by the kernels over the level windows (algorithmic
+        // point-updates: the long-window passes do ~3x this on 256 threads)
+        st.refine_point_updates = (int64_t)hh->refine_updates;
+        st.fp64_point_updates = (int64_t)hh->df_updates;
     }
     ctx->stats = st;
 

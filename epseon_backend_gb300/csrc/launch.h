@@ -17,6 +17,8 @@ struct DevBatch {
     const double* V64;         // concatenated potentials
     double* W64;               // a V (FP64)
     double* Msuf;              // suffix minima of V on i0..i1
+    double* Mpre;              // prefix minima of V on i0..i1 (fast method), or nullptr
+    float* Bmin;               // minima of W over 32-point blocks (index offf / 32 + block; fast method)
     float2* Wf2;               // a V as (hi, lo) floats, tile-aligned per potential
     int32_t* counts;           // [n * n_trial]
     LevelWork* levels;         // [max_levels]
@@ -87,12 +89,13 @@ void launch_gather(const DevBatch& b, int32_t* n_total, int32_t* n_out, double* 
 void launch_newton_df(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_norm_df(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_write_df(const DevBatch& b, int sm_count, cudaStream_t s);
-void launch_fallback_df(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_twist_df(const DevBatch& b, int sm_count, cudaStream_t s);
+void launch_scale_psi(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_twist64(const DevBatch& b, int sm_count, cudaStream_t s);
 
 // longwin.cu
 void launch_refine_long(const DevBatch& b, int sm_count, cudaStream_t s);
+void launch_fallback_long(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_norm_long(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_write_long(const DevBatch& b, int sm_count, cudaStream_t s);
 

@@ -394,6 +394,7 @@ __global__ void __launch_bounds__(kLevelThreads) refine32_kernel(DevBatch b) {
         w.k = k;
         w.norm_k_in = sum;  // sum psi~^2 at the match point k, the Newton denominator of newton_df
         w.iters = it;
+        atomicAdd(&b.hdr->refine_updates, (unsigned long long)(it + 1) * (unsigned long long)(w.j1 - w.j0));
         b.levels[slot] = w;
     }
 }
@@ -578,7 +579,7 @@ __global__ void gather_kernel(DevBatch b, int32_t* n_total, int32_t* n_out, doub
             const LevelWork w = b.levels[m.level_base + s];
             energy[o] = (apply_dE && fabs(w.dE) <= 1e-9) ? w.E + w.dE : w.E;
             nodes[o] = w.nodes;
-            status[o] = w.status | (m.status & EPSCU_STATUS_UNDER);
+            status[o] = (w.status & EPSCU_STATUS_PUBLIC) | (m.status & EPSCU_STATUS_UNDER);
             if (err_est) err_est[o] = fabs(w.dE);
         } else {
             energy[o] = NAN;

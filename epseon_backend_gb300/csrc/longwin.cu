@@ -30,7 +30,10 @@
 // Kernels (one CTA per long level, levels from the long list the window
 // kernel fills; the lane-per-level kernels skip these levels):
 //   refine_long : safeguarded Cooley-Newton in double-float from the scan
-//                 bracket to 1e-12 (replaces refine32 + newton_df + fallback);
+//                 bracket to 1e-12 (replaces refine32 + newton_df); run again
+//                 over the levels newton_df could not settle (the fallback:
+//                 any window length, from the scan bracket widened by one
+//                 trial spacing);
 //   norm_long   : the norm pass and its match-point candidates (as norm_df);
 //   write_long  : psi to HBM (as write_df).
 #include <cuda_runtime.h>
@@ -423,11 +426,13 @@ __device__ __forceinline__ bool cancelled(const DevBatch& b) { return b.cancel &
 // sees the level's own node count (so a neighbouring level cannot attract
 // the iteration) and stay inside the bracket, bisection otherwise.  After the
 // match point moves to the peak of |psi| the pass is redone at the same E.
-__global__ void __launch_bounds__(kLongThreads) refine_long_kernel(DevBatch b) {
+// fallback = 0: the long list; 1: the levels newton_df handed over.
+__global__ void __launch_bounds__(kLongThreads) refine_long_kernel(DevBatch b, int fallback) {
     __shared__ LongShared sh;
-    const int n = min(b.hdr->n_long, b.max_levels);
+    const int n = fallback ? min(b.hdr->fallbacks, b.max_levels) : min(b.hdr->n_long, b.max_levels);
+    const int32_t* list = fallback ? b.fallback_list : b.long_list;
     for (int q = blockIdx.x; q < n; q += gridDim.x) {
-        const int slot = b.long_list[q];
+        const int slot = list[q];
         LevelWork w = b.levels[slot];
         if (w.status & EPSCU_STATUS_NOTFOUND) continue;
         if (cancelled(b)) {
@@ -438,6 +443,13 @@ __global__ void __launch_bounds__(kLongThreads) refine_long_kernel(DevBatch b) {
         const float2* Wf = b.Wf2 + m.offf;
         const double* W = b.W64 + m.off;
         double lo = w.lo, hi = w.hi, E = w.E, sum = 1.0;
+        if (fallback) {
+            // the FP32 bracket may be off by its count errors: restart from
+            // the scan bracket widened by one trial spacing (inside the window)
+            lo = fmax(m.e_lo, w.lo0 - m.delta);
+            hi = fmin(m.e_cap, w.hi0 + m.delta);
+            if (!(E > lo && E < hi)) E = 0.5 * (lo + hi);
+        }
         int k = clamp_k(w, match_index(m, b.Msuf, E));
         bool done = false, moved_last = false;
         int it = 0;
@@ -472,12 +484,14 @@ __global__ void __launch_bounds__(kLongThreads) refine_long_kernel(DevBatch b) {
         }
         if (threadIdx.x == 0) {
             if (!done) w.status |= EPSCU_STATUS_MAXITER;
+            w.status &= ~EPSCU_STATUS_FALLBACK;
             w.lo = lo;
             w.hi = hi;
             w.E = E;
             w.k = k;
             w.norm_k_in = sum;
             w.iters = it;
+            atomicAdd(&b.hdr->df_updates, (unsigned long long)(it + 1) * (unsigned long long)(w.j1 - w.j0));
             b.levels[slot] = w;
         }
         __syncthreads();
@@ -513,6 +527,11 @@ __global__ void __launch_bounds__(kLongThreads) norm_long_kernel(DevBatch b) {
                 r = r2;
                 k = k2;
             }
+        }
+        if (redo_norm(w, r)) {
+            if (threadIdx.x == 0) atomicAdd(&b.hdr->n_redo, 1);
+            w.E += r.dE;
+            r = long_pass<1>(m, w, Wf, W, w.E, k, 1.0, sh);
         }
         finalize_df(m, w, r, k);
         if (threadIdx.x == 0) {
@@ -553,7 +572,11 @@ __global__ void __launch_bounds__(kLongThreads) write_long_kernel(DevBatch b) {
 
 void launch_refine_long(const DevBatch& b, int sm_count, cudaStream_t s) {
     if (!b.long_list) return;
-    refine_long_kernel<<<sm_count * 2, kLongThreads, 0, s>>>(b);
+    refine_long_kernel<<<sm_count * 2, kLongThreads, 0, s>>>(b, 0);
+}
+void launch_fallback_long(const DevBatch& b, int sm_count, cudaStream_t s) {
+    if (!b.fallback_list) return;
+    refine_long_kernel<<<sm_count * 2, kLongThreads, 0, s>>>(b, 1);
 }
 void launch_norm_long(const DevBatch& b, int sm_count, cudaStream_t s) {
     if (!b.long_list) return;

@@ -10,11 +10,16 @@
 // instructions (~1000 FP32-issue equivalents on GB300) for the same pass in
 // native FP64.
 //
-//  newton_df : Cooley corrections from the FP32 energy (usually one pass) in an
-//              FP64 count bracket; levels that do not settle go to
-//  fallback_df: multisection on compensated-FP32 counts, one warp per level.
-//  norm_df   : sums, node count, peak of |psi| and the constants of the write.
-//  write_df  : recomputes the pass and writes psi (FP64) to HBM.
+//  newton_df : Cooley corrections from the FP32 energy (one or two passes) in
+//              an FP64 count bracket; levels that do not settle go to the
+//              CTA-per-level Newton of longwin.cu (the fallback).
+//  norm_df   : sums, node count, peak of |psi| and the constants of the
+//              write; with psi requested its final pass also stores the
+//              unnormalised psi-hat in the level's row, and
+//  scale_psi : applies the constants (one HBM pass over the rows).
+//  twist_df  : twist-index match point for the levels norm_df flagged.
+//  write_df  : recomputes psi from the stored constants (the adjoint's
+//              recompute path).
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -31,12 +36,13 @@ namespace {
 constexpr int kThreads = 128;
 
 // MODE 0: state only (Newton)   MODE 1: + sums, psi-hat, peak   MODE 2: + write
+// MODE 3: MODE 1 + psi-hat written unnormalised (absolute scale, FP64)
 template <int MODE>
 struct SideDF {
     dfl A, D, q;      // state ~ s (u_i, u_i - u_{i-1}); q = 1/s (MODE >= 1)
     int eA, eQ;       // exponents removed from (A, D) and from q
     int nodes;
-    double S;         // MODE 1: sum of psi-hat^2 in the current stored scale (FP64)
+    double S;         // MODE 1/3: sum of psi-hat^2 in the current stored scale (FP64)
     int peak_L, peak_i;
 };
 
@@ -54,6 +60,7 @@ __device__ __forceinline__ void side_df(const float2* __restrict__ Wf, dfl aE, i
     dfl Sacc = {0.0f, 0.0f};
     dfl F = {0.0f, 0.0f};
     if (MODE == 2) F = df_from_double(L * ldexp(1.0, min(1000, max(-1100, -Xk))));
+    double sc = 1.0;  // MODE 3: 2^(eA + eQ), the absolute scale of psi-hat
     const int nsteps = (to - from) * dir;
     auto load8 = [&](float2* w8, int base) {
 #pragma unroll
@@ -71,10 +78,11 @@ __device__ __forceinline__ void side_df(const float2* __restrict__ Wf, dfl aE, i
                 const dfl f = df_add({1.0f, 0.0f}, T);
                 const dfl qn = df_mul(st.q, df_recip(f));
                 const dfl psi = df_mul(st.A, qn);  // psi-hat_i = A_i / s_{i+1}
-                if (MODE == 1) {
+                if (MODE == 1 || MODE == 3) {
                     const float p = __fmul_rn(psi.h, psi.h);
                     const float e = __fmaf_rn(psi.h, psi.h, -p);
                     Sacc = df_add(Sacc, {p, __fmaf_rn(2.0f * psi.h, psi.l, e)});
+                    if (MODE == 3) out[i] = (f2d(psi.h) + f2d(psi.l)) * sc;
                 } else {
                     const dfl v = df_mul(psi, F);
                     out[i] = f2d(v.h) + f2d(v.l);
@@ -102,7 +110,8 @@ __device__ __forceinline__ void side_df(const float2* __restrict__ Wf, dfl aE, i
             eq = max(-120, min(120, fexp(st.q.h)));
             st.q = df_scale(st.q, fpow2(-eq));
             st.eQ += eq;
-            if (MODE == 1) {
+            if (MODE == 3 && e + eq != 0) sc = pow2(max(-1000, min(1000, st.eA + st.eQ)));
+            if (MODE == 1 || MODE == 3) {
                 // flush the block sum into FP64 in the old scale, then rescale
                 st.S = (st.S + (f2d(Sacc.h) + f2d(Sacc.l))) * ldexp(1.0, -2 * (e + eq));
                 Sacc = {0.0f, 0.0f};
@@ -126,18 +135,20 @@ __device__ __forceinline__ void side_df(const float2* __restrict__ Wf, dfl aE, i
         load8(w8, base);
         run8(w8, base);
     }
-    if (MODE == 1) st.S += f2d(Sacc.h) + f2d(Sacc.l);
+    if (MODE == 1 || MODE == 3) st.S += f2d(Sacc.h) + f2d(Sacc.l);
 }
 
 // one pass at E with match point k over the level's window [w.j0, w.j1];
-// MODE 0: gamma/count only, MODE 1: + sums
+// MODE 0: gamma/count only, MODE 1: + sums, MODE 3: + unnormalised psi-hat
+// into row (the level's psi row)
 template <int MODE>
 __device__ PassDF pass_df(const PotMeta& m, const LevelWork& w, const float2* __restrict__ Wf,
-                          const double* __restrict__ W64, double E, int k, double sum_fallback) {
+                          const double* __restrict__ W64, double E, int k, double sum_fallback,
+                          double* __restrict__ row = nullptr) {
     const dfl aE = energy_df(m, E);
     SideDF<MODE> o, in;
-    side_df<MODE>(Wf, aE, w.j0, k, +1, o, nullptr, 0.0, 0);
-    side_df<MODE>(Wf, aE, w.j1, k, -1, in, nullptr, 0.0, 0);
+    side_df<MODE>(Wf, aE, w.j0, k, +1, o, row, 0.0, 0);
+    side_df<MODE>(Wf, aE, w.j1, k, -1, in, row, 0.0, 0);
     const double Tk = __dsub_rn(__dmul_rn(m.a, E), __ldg(W64 + k));
     const double fk = 1.0 + Tk;
     const double Ao = df_to_double(o.A), Do = df_to_double(o.D);
@@ -151,7 +162,7 @@ __device__ PassDF pass_df(const PotMeta& m, const LevelWork& w, const float2* __
     r.peak_log2 = 0;
     r.pk_out = r.pk_in = 0.0;
     r.ex_out = r.ex_in = 0;
-    if (MODE == 1) {
+    if (MODE == 1 || MODE == 3) {
         // psi-hat at k from each side: A_k q_k / f_k
         const double rfk = 1.0 / fk;
         r.pk_out = Ao * df_to_double(o.q) * rfk;
@@ -171,6 +182,13 @@ __device__ PassDF pass_df(const PotMeta& m, const LevelWork& w, const float2* __
     return r;
 }
 
+// the level's psi row for the fused norm/write, or nullptr (no psi requested,
+// or the psi buffer overflowed: the level setup raised the capacity error)
+__device__ __forceinline__ double* psi_row(const DevBatch& b, const PotMeta& m, const LevelWork& w) {
+    if (!b.psi || b.hdr->error) return nullptr;
+    return b.psi + m.psi_off + (int64_t)(w.v - b.min_level) * m.N;
+}
+
 __global__ void __launch_bounds__(kThreads, 4) newton_df_kernel(DevBatch b) {
     for (int2 unit; next_unit(b, kQNewtonDF, unit);) {
         if ((int)(threadIdx.x & 31) >= unit.y) continue;
@@ -183,15 +201,19 @@ __global__ void __launch_bounds__(kThreads, 4) newton_df_kernel(DevBatch b) {
         double E = w.E;
         double lo = w.lo - 1e-8, hi = w.hi + 1e-8;
         bool ok = false;
+        int n_pass = 0;
         for (int it = 0; it < 4 && !ok; ++it) {
             const PassDF r = pass_df<0>(m, w, Wf, W, E, w.k, w.norm_k_in);
+            ++n_pass;
             if (r.count > w.v) hi = fmin(hi, E);
             else lo = fmax(lo, E);
             const double En = E + r.dE;
             if (!isfinite(En) || !(En >= lo && En <= hi) || r.nodes != w.v) break;
-            // from the FP32 energy (~1e-9) one step is enough: quadratic
-            // convergence leaves ~1e-13, and norm_df applies one more correction
-            ok = fabs(r.dE) <= (it == 0 ? 1e-8 : 1e-12 * fmax(1.0, fabs(E)));
+            // the step divides by the FP32 pass's sum psi~^2 (relative error up
+            // to ~1e-4 on long windows), so it leaves ~1e-4 |dE|: one step is
+            // enough from within 1e-10, and the norm pass corrects the rest.
+            // (A pass with its own sum costs ~1.5x: measured slower overall.)
+            ok = fabs(r.dE) <= (it == 0 ? 1e-10 : 1e-12 * fmax(1.0, fabs(E)));
             E = En;
         }
         if (!ok) {
@@ -203,58 +225,8 @@ __global__ void __launch_bounds__(kThreads, 4) newton_df_kernel(DevBatch b) {
         } else {
             w.E = E;
         }
+        atomicAdd(&b.hdr->df_updates, (unsigned long long)n_pass * (unsigned long long)(w.j1 - w.j0));
         b.levels[slot] = w;
-    }
-}
-
-// Multisection on compensated-FP32 twisted Sturm counts for the levels the
-// Newton stage could not settle (near-degenerate pairs, match points across a
-// barrier).  One warp per level: lane j counts at lo + (j+1)(hi-lo)/33 and a
-// ballot picks the sub-interval holding the level, so every round gains five
-// bits instead of one.  The FP32 bracket widened by 2e-8 is verified first;
-// the scan bracket widened by one trial spacing is the fallback.
-__global__ void __launch_bounds__(128) fallback_df_kernel(DevBatch b) {
-    const int n = min(b.hdr->fallbacks, b.max_levels);
-    const int lane = threadIdx.x & 31;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int n_warps = (gridDim.x * blockDim.x) >> 5;
-    for (int q = warp; q < n; q += n_warps) {
-        const int slot = b.fallback_list[q];
-        LevelWork w = b.levels[slot];
-        const PotMeta m = b.meta[w.p];
-        const float2* Wf = b.Wf2 + m.offf;
-        const double* W = b.W64 + m.off;
-        double lo = fmax(m.e_lo, w.lo - 2e-8), hi = fmin(m.e_cap, w.hi + 2e-8);
-        {
-            // lane 0 checks lo, lane 1 checks hi
-            const double Ec = lane == 0 ? lo : hi;
-            const int c = lane < 2 ? pass_df<0>(m, w, Wf, W, Ec, w.k, 1.0).count : 0;
-            const int c_lo = __shfl_sync(0xffffffffu, c, 0), c_hi = __shfl_sync(0xffffffffu, c, 1);
-            if (!(c_lo <= w.v && c_hi > w.v)) {
-                lo = fmax(m.e_lo, w.lo0 - m.delta);
-                hi = fmin(m.e_cap, w.hi0 + m.delta);
-            }
-        }
-        for (int round = 0; round < 16; ++round) {
-            if (hi - lo <= 1e-12 * fmax(1.0, fabs(lo))) break;
-            const double step = (hi - lo) / 33.0;
-            const double Ej = lo + (lane + 1) * step;
-            const bool above = pass_df<0>(m, w, Wf, W, Ej, w.k, 1.0).count > w.v;
-            const unsigned mask = __ballot_sync(0xffffffffu, above);
-            // counts are monotone in E: the first lane above bounds the level
-            const int first = mask ? __ffs(mask) - 1 : 32;
-            const double nlo = first == 0 ? lo : lo + first * step;
-            const double nhi = first == 32 ? hi : lo + (first + 1) * step;
-            lo = nlo;
-            hi = nhi;
-        }
-        if (lane == 0) {
-            w.E = 0.5 * (lo + hi);
-            w.lo = lo;
-            w.hi = hi;
-            w.status &= ~EPSCU_STATUS_FALLBACK;
-            b.levels[slot] = w;
-        }
     }
 }
 
@@ -267,29 +239,47 @@ __global__ void __launch_bounds__(kThreads, 4) norm_df_kernel(DevBatch b) {
         const PotMeta m = b.meta[w.p];
         const float2* Wf = b.Wf2 + m.offf;
         const double* W = b.W64 + m.off;
+        // with psi requested every pass also stores its unnormalised psi-hat
+        // in the level's row; scale_psi applies the constants afterwards
+        double* row = psi_row(b, m, w);
+        int n_pass = 0;
+        auto pass = [&](int kk) {
+            ++n_pass;
+            return row ? pass_df<3>(m, w, Wf, W, w.E, kk, 1.0, row) : pass_df<1>(m, w, Wf, W, w.E, kk, 1.0);
+        };
         // match point candidates: the FP32 one, the peak of |psi| seen by this
         // pass, the outer turning point and its peak; the first whose
         // stitched solution has v nodes wins
         int k = w.k;
-        PassDF r = pass_df<1>(m, w, Wf, W, w.E, k, 1.0);
+        PassDF r = pass(k);
         if (r.peak_log2 >= 2) {
             k = clamp_k(w, r.peak_i);
-            r = pass_df<1>(m, w, Wf, W, w.E, k, 1.0);
+            r = pass(k);
         }
+        int k_row = k;  // the pass whose psi-hat the row holds
         if (r.nodes != w.v) {
             const int kt = clamp_k(w, match_index(m, b.Msuf, w.E));
-            PassDF r2 = pass_df<1>(m, w, Wf, W, w.E, kt, 1.0);
+            PassDF r2 = pass(kt);
             int k2 = kt;
             if (r2.nodes != w.v && r2.peak_log2 >= 1) {
                 k2 = clamp_k(w, r2.peak_i);
-                r2 = pass_df<1>(m, w, Wf, W, w.E, k2, 1.0);
+                r2 = pass(k2);
             }
+            k_row = k2;
             if (r2.nodes == w.v) {
                 r = r2;
                 k = k2;
             }
         }
+        if (redo_norm(w, r)) {
+            atomicAdd(&b.hdr->n_redo, 1);
+            w.E += r.dE;
+            r = pass(k);
+        } else if (row && k_row != k) {
+            r = pass(k);
+        }
         finalize_df(m, w, r, k);
+        atomicAdd(&b.hdr->df_updates, (unsigned long long)n_pass * (unsigned long long)(w.j1 - w.j0));
         if (suspicious(m, w, r.nodes, r.dE) && b.twist_list) {
             const int q = atomicAdd(&b.hdr->n_twist, 1);
             if (q < b.max_twist) b.twist_list[q] = slot;
@@ -370,12 +360,16 @@ __global__ void __launch_bounds__(64) twist_df_kernel(DevBatch b) {
         // Newton at the new match point: the energy was settled at the old one,
         // so its Cooley correction here may still be above the tolerance
         double E1 = w.E;
-        PassDF r = pass_df<1>(m, w, Wf, W, E1, k, 1.0);
+        double* row = is_long(w) ? nullptr : psi_row(b, m, w);  // long rows: write_long
+        auto pass = [&](double Ep) {
+            return row ? pass_df<3>(m, w, Wf, W, Ep, k, 1.0, row) : pass_df<1>(m, w, Wf, W, Ep, k, 1.0);
+        };
+        PassDF r = pass(E1);
         for (int it = 0; it < 8; ++it) {
             if (r.nodes != w.v || !isfinite(r.dE) || !(fabs(r.dE) < 1e-7)) break;
-            if (fabs(r.dE) <= 1e-12 * fmax(1.0, fabs(E1))) break;
+            if (fabs(r.dE) <= 1e-13 * fmax(1.0, fabs(E1))) break;
             E1 += r.dE;
-            r = pass_df<1>(m, w, Wf, W, E1, k, 1.0);
+            r = pass(E1);
         }
         w.E = E1;
         finalize_df(m, w, r, k);
@@ -415,7 +409,43 @@ __global__ void __launch_bounds__(kThreads, 4) write_df_kernel(DevBatch b) {
     }
 }
 
+// The write-back of the fused norm/write: each row holds the unnormalised
+// psi-hat of the final norm pass on [j0, k) and (k, j1]; scale it by the
+// side constants (norm_k 2^-ex), set psi_k = ck and zero the rest of the row.
+// One warp per level, coalesced: HBM-bound (8 B read + 8 B written per window
+// point, 8 B written elsewhere).
+__global__ void __launch_bounds__(256) scale_psi_kernel(DevBatch b) {
+    if (!b.psi || b.hdr->error) return;
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int n_warps = (gridDim.x * blockDim.x) >> 5;
+    const int total = b.hdr->total_levels;
+    for (int slot = warp; slot < total; slot += n_warps) {
+        const LevelWork w = b.levels[slot];
+        if (is_long(w)) continue;  // written by write_long
+        const PotMeta m = b.meta[w.p];
+        double* row = b.psi + m.psi_off + (int64_t)(w.v - b.min_level) * m.N;
+        if (no_result(w)) {
+            for (int i = lane; i < m.N; i += 32) row[i] = 0.0;
+            continue;
+        }
+        const double c_out = w.norm_k_out * pow2(max(-1000, min(1000, -w.ex_out)));
+        const double c_in = w.norm_k_in * pow2(max(-1000, min(1000, -w.ex_in)));
+        for (int i = lane; i < m.N; i += 32) {
+            double v = 0.0;
+            if (i >= w.j0 && i < w.k) v = row[i] * c_out;
+            else if (i > w.k && i <= w.j1) v = row[i] * c_in;
+            else if (i == w.k) v = w.ck;
+            row[i] = v;
+        }
+    }
+}
+
 }  // namespace
+
+void launch_scale_psi(const DevBatch& b, int sm_count, cudaStream_t s) {
+    scale_psi_kernel<<<sm_count * 8, 256, 0, s>>>(b);
+}
 
 void launch_newton_df(const DevBatch& b, int sm_count, cudaStream_t s) {
     newton_df_kernel<<<sm_count * 8, kThreads, 0, s>>>(b);
@@ -428,9 +458,6 @@ void launch_write_df(const DevBatch& b, int sm_count, cudaStream_t s) {
 }
 void launch_twist_df(const DevBatch& b, int sm_count, cudaStream_t s) {
     twist_df_kernel<<<sm_count, 64, 0, s>>>(b);
-}
-void launch_fallback_df(const DevBatch& b, int sm_count, cudaStream_t s) {
-    fallback_df_kernel<<<sm_count * 2, 128, 0, s>>>(b);
 }
 
 }  // namespace epscu

@@ -133,6 +133,35 @@ __global__ void __launch_bounds__(kPrepThreads) prepare_kernel(DevBatch b) {
         M[i] = run;
     }
 
+    if (b.Mpre) {
+        // prefix minima (left to right) and minima of a V over 32-point blocks
+        // clipped to [i0, i1], rounded down to float: the decay-window bounds
+        __syncthreads();
+        chunk_min[tid] = cm;
+        __syncthreads();
+        if (tid == 0) {
+            double acc = INFINITY;
+            for (int t = 0; t < nt; ++t) {
+                const double x = chunk_min[t];
+                chunk_min[t] = acc;  // minimum of all chunks to the left of t
+                acc = fmin(acc, x);
+            }
+        }
+        __syncthreads();
+        double* P = b.Mpre + m.off;
+        double pr = chunk_min[tid];
+        for (int i = c0; i < c1; ++i) {
+            pr = fmin(pr, V[i]);
+            P[i] = pr;
+        }
+        float* Bm = b.Bmin + m.offf / 32;
+        for (int B = (i0 >> 5) + tid; B <= (i1 >> 5); B += nt) {
+            double vb = INFINITY;
+            for (int i = max(B << 5, i0); i <= min((B << 5) + 31, i1); ++i) vb = fmin(vb, V[i]);
+            Bm[B] = __double2float_rd(__dmul_rn(a, vb));
+        }
+    }
+
     if (tid == 0) {
         int status = 0;
         if (bad) status |= EPSCU_STATUS_BAD | EPSCU_STATUS_NONFINITE;
@@ -296,26 +325,109 @@ __global__ void bracket_kernel(DevBatch b) {
     }
 }
 
+// Decay window at energy Eu (fast method; one call per warp, all lanes).
+// Beyond the classical turning points of Eu (V > Eu there) the discrete
+// solution decays at least by the constant-coefficient rate of the Numerov
+// recurrence, acosh(1 + 6 t_i) per step with t_i = W_i - a Eu (for small t it
+// is kappa h, the WKB exponent; for larger t it is below the true rate).  The
+// window ends where that exponent, summed from the turning point, reaches
+// `decay`: Dirichlet ends there change the solution by about e^-decay relative
+// to its size at the turning point and an eigenvalue by a relative e^-2 decay,
+// and every energy below Eu has a narrower window.  The classical choice of
+// the start of the inward integration in Numerov-Cooley codes.
+// Turning points come from binary searches on the suffix and prefix minima of
+// V; the sums run over whole 32-point blocks beyond the turning point's block,
+// a block of n points counting n acosh(1 + 6 (min W - a Eu)) (block minima
+// rounded down, a Eu rounded up): a lower bound of the decay, so the window
+// can only come out wider.  Returns [j0, j1] within [i0, i1].
+__device__ int2 decay_window(const PotMeta& m, const DevBatch& b, double Eu, float decay) {
+    const int lane = threadIdx.x & 31;
+    const unsigned full = 0xffffffffu;
+    const float aEu = __double2float_ru(m.a * Eu);
+    const float* Bm = b.Bmin + m.offf / 32;
+    const int t_out = match_index(m, b.Msuf, Eu);
+    int t_in;
+    {
+        // first i with min(V_i0 .. V_i) <= Eu (the prefix minima do not increase)
+        const double* P = b.Mpre + m.off;
+        int lo = m.i0, hi = m.i1;
+        while (lo < hi) {
+            const int mid = lo + (hi - lo) / 2;
+            if (P[mid] <= Eu) hi = mid;
+            else lo = mid + 1;
+        }
+        t_in = lo;
+    }
+    const int B_first = m.i0 >> 5, B_last = m.i1 >> 5;
+    auto block_decay = [&](int B) {
+        const int n = min((B << 5) + 31, m.i1) - max(B << 5, m.i0) + 1;
+        return (float)n * acoshf(1.0f + 6.0f * fmaxf(Bm[B] - aEu, 0.0f));
+    };
+    int j1 = m.i1;
+    float X = 0.0f;
+    for (int B0 = (t_out >> 5) + 1; B0 <= B_last; B0 += 32) {
+        const int B = B0 + lane;
+        float s = B <= B_last ? block_decay(B) : 0.0f;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const float y = __shfl_up_sync(full, s, o);
+            if (lane >= o) s += y;
+        }
+        const unsigned hit = __ballot_sync(full, B <= B_last && X + s >= decay);
+        if (hit) {
+            j1 = min(((B0 + __ffs(hit) - 1) << 5) + 31, m.i1);
+            break;
+        }
+        X += __shfl_sync(full, s, 31);
+    }
+    int j0 = m.i0;
+    X = 0.0f;
+    for (int B0 = (t_in >> 5) - 1; B0 >= B_first; B0 -= 32) {
+        const int B = B0 - lane;
+        float s = B >= B_first ? block_decay(B) : 0.0f;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const float y = __shfl_up_sync(full, s, o);
+            if (lane >= o) s += y;
+        }
+        const unsigned hit = __ballot_sync(full, B >= B_first && X + s >= decay);
+        if (hit) {
+            j0 = max((B0 - (__ffs(hit) - 1)) << 5, m.i0);
+            break;
+        }
+        X += __shfl_sync(full, s, 31);
+    }
+    if (j1 - j0 < 4) return make_int2(m.i0, m.i1);
+    return make_int2(j0, j1);
+}
+
 // Decay window of every level slot (fast method), at E_up = hi0 + 2 delta:
 // an energy above every energy the level's passes use (bracket, Newton steps,
 // the fallback's widened bracket), so one window serves all of them.  Levels
-// whose window is longer than kLongWindow go to the long list (CTA-per-level
-// passes).  One warp per level.
-__global__ void __launch_bounds__(128) window_kernel(DevBatch b) {
+// whose window is longer than kLongWindow (or kFewWindow in a batch of few
+// levels) go to the long list (CTA-per-level passes).  One warp per level.
+// (Sharing one window per warp unit would keep the lanes' loads of W
+// warp-wide broadcasts, but the unit's widest window costs more point-updates
+// than the divergent loads: measured slower on the mixed batch.)
+__global__ void __launch_bounds__(128) window_kernel(DevBatch b, int sm_count) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int n_warps = (gridDim.x * blockDim.x) >> 5;
     const int total = b.hdr->total_levels;
+    const int long_min = total <= kFewLevelsPerSM * sm_count ? kFewWindow : kLongWindow;
     for (int slot = warp; slot < total; slot += n_warps) {
         const LevelWork w = b.levels[slot];
         if (w.status & EPSCU_STATUS_NOTFOUND) continue;
         const PotMeta m = b.meta[w.p];
-        const int2 jw = decay_window(m, b.W64 + m.off, b.Msuf, w.hi0 + 2.0 * m.delta, kWindowDecay);
+        const int2 jw = decay_window(m, b, w.hi0 + 2.0 * m.delta, kWindowDecay);
         if ((threadIdx.x & 31) == 0) {
             b.levels[slot].j0 = jw.x;
             b.levels[slot].j1 = jw.y;
-            if (jw.y - jw.x > kLongWindow && b.long_list) {
+            if (jw.y - jw.x > long_min && b.long_list) {
                 const int q = atomicAdd(&b.hdr->n_long, 1);
-                if (q < b.max_levels) b.long_list[q] = slot;
+                if (q < b.max_levels) {
+                    b.long_list[q] = slot;
+                    b.levels[slot].status = w.status | EPSCU_STATUS_LONG;
+                }
             }
         }
     }
@@ -334,7 +446,7 @@ __global__ void __launch_bounds__(128) scan_window_kernel(DevBatch b, int n_blk)
         int2 jw = make_int2(m.i0, m.i1);
         if (!(m.status & EPSCU_STATUS_BAD)) {
             const int j = min((q + 1) * kScanWinBlock, b.n_trial) - 1;
-            jw = decay_window(m, b.W64 + m.off, b.Msuf, trial_energy(m, j), kWindowDecay);
+            jw = decay_window(m, b, trial_energy(m, j), kWindowDecay);
         }
         if ((threadIdx.x & 31) == 0) b.scan_win[e] = jw;
     }
@@ -427,7 +539,7 @@ void launch_level_setup(const DevBatch& b, cudaStream_t s) {
 }
 
 void launch_window(const DevBatch& b, int sm_count, cudaStream_t s) {
-    window_kernel<<<sm_count * 8, 128, 0, s>>>(b);
+    window_kernel<<<sm_count * 8, 128, 0, s>>>(b, sm_count);
 }
 
 void launch_scan_window(const DevBatch& b, int sm_count, cudaStream_t s) {

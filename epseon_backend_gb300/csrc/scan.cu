@@ -229,7 +229,10 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
         const int item = s_item;
         if (item >= n_items || s_abort) break;
         const int p = b.order[item / ipp];
-        const int j = (item % ipp) * THREADS + tid;
+        // energy blocks highest first: windows (and so the work) grow with
+        // the energy, so the longest items of a potential start first
+        const int blk = ipp - 1 - item % ipp;
+        const int j = blk * THREADS + tid;
         const PotMeta m = b.meta[p];
         if (m.status & EPSCU_STATUS_BAD) {
             if (j < b.n_trial) b.counts[(int64_t)p * b.n_trial + j] = 0;
@@ -240,7 +243,7 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
         int j0 = m.i0, j1 = m.i1;
         if (b.scan_win) {
             const int nb = (b.n_trial + kScanWinBlock - 1) / kScanWinBlock;
-            const int e0 = (item % ipp) * THREADS;
+            const int e0 = blk * THREADS;
             const int q0 = e0 / kScanWinBlock, q1 = min(nb - 1, (e0 + THREADS - 1) / kScanWinBlock);
             j0 = m.i1;
             j1 = m.i0;
@@ -254,7 +257,7 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
         }
         const TileSeq seq = make_seq(j0, j1, m.k_scan, TILE);
         if (tid == 0) {
-            const int n_e = min(THREADS, b.n_trial - (item % ipp) * THREADS);
+            const int n_e = min(THREADS, b.n_trial - blk * THREADS);
             atomicAdd(&b.hdr->scan_updates, (unsigned long long)n_e * (unsigned long long)(j1 - j0));
         }
         const int L = seq.size();

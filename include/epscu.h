@@ -201,18 +201,22 @@ epscu_status epscu_tabulate(epscu_ctx* ctx, int32_t n, const int32_t* kind, cons
 epscu_status epscu_cancel(epscu_ctx* ctx);
 
 /* Timing of the last solve: per-stage milliseconds (CUDA events on the solve
- * stream) and the counters the roofline uses. */
+ * stream) and the counters the roofline uses.  Stages: prepare (set-up and,
+ * for the fast method, the scan's decay windows), scan (the scan kernel
+ * alone), refine32 (fast: level windows, FP32 refinement and the long-window
+ * Newton), polish (Newton, fallback, norm and twist passes; plain: bisection,
+ * norm, twist), write (psi write-back). */
 typedef struct epscu_stats {
     float ms_prepare, ms_scan, ms_refine32, ms_polish64, ms_write, ms_total;
     int64_t scan_point_updates;    /* trial energies x points of the scan (its window for the fast method) */
-    int64_t refine_point_updates;  /* FP32 refinement passes x points */
-    int64_t fp64_point_updates;    /* FP64 passes x points */
+    int64_t refine_point_updates;  /* FP32 refinement passes x points (fast method) */
+    int64_t fp64_point_updates;    /* FP64 passes x points (plain); double-float passes x points (fast) */
     int64_t psi_bytes;             /* wavefunction bytes written */
     int64_t n_levels;              /* levels solved */
     int32_t kernel_launches;       /* kernels launched by the solve */
     int32_t fallbacks;             /* levels that needed the bisection fallback */
     int32_t twist_searches;        /* levels re-matched by the twist-index search */
-    int32_t reserved;
+    int32_t norm_redos;            /* norm passes redone at E + dE (fast method) */
 } epscu_stats;
 epscu_status epscu_last_stats(epscu_ctx* ctx, epscu_stats* stats);
 

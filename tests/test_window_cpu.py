@@ -4,8 +4,8 @@ The fast method's scan and per-level passes run on a window [j0, j1] of the
 grid instead of the oracle's [i0, i1]: beyond the classical turning points of
 an energy E_up the discrete solution decays at least by acosh(1 + 6 t_i) per
 step (t_i = a (V_i - E_up)), and the window ends where that exponent, summed
-from the turning point, reaches 46.  This file restates the rule in numpy (in
-FP64; the kernels sum it in FP32, which moves an end by a point or two) and
+from the turning point, reaches 46.  This file restates the kernels' rule in
+numpy (in FP64; the kernels sum it in FP32 with block minima rounded down) and
 checks on dense eigen-decompositions of the discrete problem that the cut
 leaves every eigenvalue below E_up unchanged to FP64 rounding and the
 eigenvectors unchanged far below the 1e-8 L2 tolerance, while the window is
@@ -23,19 +23,33 @@ DECAY = 46.0
 
 
 def decay_window(V, g, mu, Eu, decay=DECAY):
-    """[j0, j1] of the kernels' decay window at energy Eu (within [i0, i1])."""
+    """[j0, j1] of the kernels' decay window at energy Eu (within [i0, i1]).
+
+    The kernels sum the decay over whole 32-point blocks beyond the block of
+    each turning point, a block of n points counting n acosh(1 + 6 t) with t
+    from the block's minimum of a V: a lower bound of the point-wise sum."""
     i0, i1, h = g.i0, g.i1, g.h
     a = mu * h * h / 6.0
-    t = a * V - a * Eu
-    d = np.arccosh(1.0 + 6.0 * np.maximum(t, 0.0))
     allowed = np.nonzero(V[i0 : i1 + 1] <= Eu)[0]
     t_in, t_out = i0 + allowed[0], i0 + allowed[-1]
-    c = np.cumsum(d[t_out + 1 : i1 + 1])
-    hit = np.nonzero(c >= decay)[0]
-    j1 = t_out + 1 + hit[0] if hit.size else i1
-    c = np.cumsum(d[i0:t_in][::-1])
-    hit = np.nonzero(c >= decay)[0]
-    j0 = t_in - 1 - hit[0] if hit.size else i0
+
+    def block_decay(B):
+        lo, hi = max(32 * B, i0), min(32 * B + 31, i1)
+        t = a * V[lo : hi + 1].min() - a * Eu
+        return (hi - lo + 1) * np.arccosh(1.0 + 6.0 * max(t, 0.0))
+
+    j1, X = i1, 0.0
+    for B in range(t_out // 32 + 1, i1 // 32 + 1):
+        X += block_decay(B)
+        if X >= decay:
+            j1 = min(32 * B + 31, i1)
+            break
+    j0, X = i0, 0.0
+    for B in range(t_in // 32 - 1, i0 // 32 - 1, -1):
+        X += block_decay(B)
+        if X >= decay:
+            j0 = max(32 * B, i0)
+            break
     if j1 - j0 < 4:
         return i0, i1
     return int(j0), int(j1)
