@@ -51,7 +51,7 @@ class Opts(C.Structure):
         ("tol", C.c_double),
         ("stream", C.c_void_p),
         ("tune", C.c_int32),
-        ("reserved", C.c_int32),
+        ("long_window", C.c_int32),
     ]
 
 
@@ -293,6 +293,7 @@ class Context:
         psi_capacity: int | None = None,
         tol: float = 1e-12,
         tune: bool = False,
+        long_window: int = 0,
     ) -> Solution:
         """Solve a batch of host potentials (host buffers through the C ABI)."""
         V, offsets, N = concat(Vs)
@@ -332,7 +333,7 @@ class Context:
             _l(psi_off),
             0,
         )
-        o = Opts(int(method), WANT_PSI if want_psi else 0, float(tol), None, 1 if tune else 0, 0)
+        o = Opts(int(method), WANT_PSI if want_psi else 0, float(tol), None, 1 if tune else 0, int(long_window))
         _check(self._lib.epscu_solve(self._h, C.byref(b), C.byref(r), C.byref(o)))
         return Solution(n_total, n_out, energy, nodes, status, err, psi, psi_off, N)
 
@@ -421,7 +422,8 @@ class DeviceBatch:
     def _ptr(self, t, ty):
         return C.cast(C.c_void_p(t.data_ptr()), ty) if t is not None else None
 
-    def solve(self, method: int = METHOD_FAST_FP32C, tune: bool = False, stage_timing: bool = False, stream=None):
+    def solve(self, method: int = METHOD_FAST_FP32C, tune: bool = False, stage_timing: bool = False, stream=None,
+              long_window: int = 0):
         import torch
 
         b = Batch(self.n, self._ptr(self.V, _dp), _l(self.offsets), _i(self.N), _d(self.r_min), _d(self.r_max),
@@ -432,7 +434,7 @@ class DeviceBatch:
                    _l(self.psi_offsets), 0)
         flags = MEM_DEVICE | (WANT_PSI if self.want_psi else 0) | (STAGE_TIMING if stage_timing else 0)
         s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
-        o = Opts(int(method), flags, 1e-12, C.c_void_p(s), 1 if tune else 0, 0)
+        o = Opts(int(method), flags, 1e-12, C.c_void_p(s), 1 if tune else 0, int(long_window))
         _check(self.ctx._lib.epscu_solve(self.ctx.handle, C.byref(b), C.byref(r), C.byref(o)))
         self.psi_required = r.psi_required
 

@@ -19,30 +19,39 @@ namespace epscu {
 
 namespace {
 
-// rows [s0, s1) of each potential are present in psi (row s at psi_off' +
-// (s - s0) N when chunked); accumulate = add into dL_dV instead of storing.
-__global__ void adjoint_kernel(DevBatch b, const double* __restrict__ gE, double* __restrict__ gV,
-                               const int64_t* __restrict__ offsets, const double* __restrict__ psi, int accumulate) {
+// psi rows of the last solve in place (row s of potential p at psi_off + s N);
+// accumulate = add into dL_dV instead of storing.  One CTA per (potential,
+// 256 points); the CTA first narrows the level loop to the levels whose
+// window meets its points (windows grow with the level, so near the ends of
+// a grid only the highest levels remain).
+__global__ void __launch_bounds__(256) adjoint_kernel(DevBatch b, const double* __restrict__ gE, double* __restrict__ gV,
+                                                      const int64_t* __restrict__ offsets, const double* __restrict__ psi,
+                                                      int accumulate) {
+    __shared__ int s_lo, s_hi;
     const int p = blockIdx.y;
     const PotMeta m = b.meta[p];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m.N) return;
+    const int i_a = blockIdx.x * blockDim.x;
+    if (i_a >= m.N) return;
+    const int i_b = min(i_a + (int)blockDim.x, m.N) - 1;
+    const LevelWork* lw = b.levels + m.level_base;
+    if (threadIdx.x == 0) {
+        s_lo = m.n_out;
+        s_hi = -1;
+    }
+    __syncthreads();
+    for (int s = threadIdx.x; s < m.n_out; s += blockDim.x) {
+        if (lw[s].j0 <= i_b && lw[s].j1 >= i_a) {
+            atomicMin(&s_lo, s);
+            atomicMax(&s_hi, s);
+        }
+    }
+    __syncthreads();
+    const int i = i_a + threadIdx.x;
+    if (i > i_b) return;
     const double* rows = psi + m.psi_off + i;
     const double* g = gE + (int64_t)p * b.level_capacity;
-    const LevelWork* lw = b.levels + m.level_base;
     double acc = 0.0;
-    int s = 0;
-    for (; s + 4 <= m.n_out; s += 4) {
-        double v[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int2 jw = make_int2(lw[s + u].j0, lw[s + u].j1);
-            v[u] = (i >= jw.x && i <= jw.y) ? __ldg(rows + (int64_t)(s + u) * m.N) : 0.0;
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) acc = fma(g[s + u] * v[u], v[u], acc);
-    }
-    for (; s < m.n_out; ++s) {
+    for (int s = s_lo; s <= s_hi; ++s) {
         if (i < lw[s].j0 || i > lw[s].j1) continue;
         const double v = __ldg(rows + (int64_t)s * m.N);
         acc = fma(g[s] * v, v, acc);

@@ -9,13 +9,25 @@
 
 namespace epscu {
 
-// Windows longer than kLongWindow points take the CTA-per-level passes of
-// longwin.cu (parallel prefix over chunks) instead of one lane per level; so
-// do windows longer than kFewWindow points when the batch has at most
-// kFewLevelsPerSM levels per SM (too few lanes to fill the GPU).
-constexpr int kLongWindow = 65536;
-constexpr int kFewWindow = 4096;
-constexpr int kFewLevelsPerSM = 4;
+// Windows longer than a threshold take the CTA-per-level passes of
+// longwin.cu (parallel prefix over chunks) instead of one lane per level.  A
+// lane marching a long window is the tail of the per-level kernels: its
+// latency, not the throughput, sets their duration; the CTA passes cost ~3x
+// the point-updates in double-float but cut the latency ~80x.  So the
+// threshold falls with the number of levels (fewer lanes to keep the GPU
+// busy): 16384 points at ~9e4 levels (the 2048-potential mixed batch),
+// proportionally less below, never under 1024 (measured on GB300: the
+// 2048-potential batch is fastest at 16384, the 64-Morse batch at 1024-2048).
+// DevBatch::long_window > 0 overrides it.
+constexpr int kLongWindow = 16384;
+constexpr int kLongWindowLevels = 90000;
+constexpr int kMinLongWindow = 1024;
+
+__host__ __device__ __forceinline__ int default_long_window(int total_levels) {
+    int w = kMinLongWindow;
+    while (w < kLongWindow && (long long)w * kLongWindowLevels < (long long)kLongWindow * total_levels) w <<= 1;
+    return w;
+}
 
 __device__ __forceinline__ bool is_long(const LevelWork& w) { return (w.status & EPSCU_STATUS_LONG) != 0; }
 

@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "epscu.h"
+#include "dfpass.cuh"
 #include "launch.h"
 
 using namespace epscu;
@@ -307,10 +308,10 @@ void enqueue_pipeline(epscu_ctx* ctx, const DevBatch& b, int method, bool want_p
         launch_fallback_long(b, ctx->sm_count, s);
         launch_norm_df(b, ctx->sm_count, s);
         launch_norm_long(b, ctx->sm_count, s);
-        launch_twist_df(b, ctx->sm_count, s);
+        launch_twist_long(b, ctx->sm_count, s);
         rec(4);
         if (want_psi) {
-            launch_scale_psi(b, ctx->sm_count, s);  // rows written unnormalised by norm_df / twist_df
+            launch_scale_psi(b, ctx->sm_count, s);  // rows written unnormalised by norm_df
             launch_write_long(b, ctx->sm_count, s);
         }
     }
@@ -448,6 +449,7 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     b.twist_scratch = (double*)ctx->get("twist_scratch", sizeof(double) * (size_t)b.max_twist * b.twist_stride, &ce);
     if (!b.twist_scratch || !b.twist_list) return fail(EPSCU_ERR_NOMEM, "device arena (twist search)");
     b.tol = opts.tol;
+    b.long_window = opts.long_window > 0 ? opts.long_window : 0;  // 0: chosen from the level count
     b.psi = nullptr;
     b.psi_capacity = 0;
     if (want_psi) {
@@ -522,12 +524,14 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     // ---- the pipeline (graph-replayed when the device-resident inputs repeat)
     const bool use_graph = dev && !stage_events;
     char keybuf[512];
+    std::string keybuf_extra;
     std::snprintf(keybuf, sizeof(keybuf), "%d|%d|%d|%d|%p|%p|%p|%p|%p|%p|%p|%p|%lld|%d|%d|%d|%d|%d|%g|%p", n,
                   batch->n_trial, batch->min_level, batch->max_level, (const void*)b.V64, (void*)b.psi,
                   (void*)o_e, (void*)o_nt, (void*)o_no, (void*)o_nd, (void*)o_st, (void*)o_err,
                   (long long)b.psi_capacity, method, cap, shape.threads, shape.tile, shape.stages, opts.tol,
                   (void*)s);  // s is the context's own stream
-    const std::string gkey = std::string(keybuf) + "|" + std::to_string(total_points);
+    keybuf_extra = std::to_string(b.long_window);
+    const std::string gkey = std::string(keybuf) + "|" + std::to_string(total_points) + "|" + keybuf_extra;
 
     auto enqueue_all = [&]() -> cudaError_t {
         cudaError_t e;
@@ -641,7 +645,7 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     // plain: prepare, scan64, level/unit setup, bracket, bisect64, norm64,
     // twist64, gather (+ write64); fast: prepare, scan window, scan32, level/unit
     // setup, bracket, window, refine32, refine_long, newton_df, fallback
-    // (refine_long over the fallback list), norm_df, norm_long, twist_df,
+    // (refine_long over the fallback list), norm_df, norm_long, twist_long,
     // gather (+ scale_psi, write_long)
     st.kernel_launches = method == EPSCU_METHOD_FAST_FP32C ? 16 + (want_psi ? 2 : 0) : 9 + (want_psi ? 1 : 0);
     if (method == EPSCU_METHOD_PLAIN_FP64) {

@@ -40,12 +40,17 @@ struct DevBatch {
     int32_t n_trial;
     int32_t min_level, max_level;
     int32_t max_N;             // longest grid of the batch
+    int32_t long_window;       // window length above which a level takes the CTA passes
     double tol;
 };
 
 // Warp-level work queue of the per-level kernels: units of up to 32
 // consecutive level slots of one potential, longest grids first.  Lane 0
 // takes the next unit and broadcasts it; false when the queue is drained.
+// (Measured slower on the mixed batch: units of levels sorted by window
+// length across potentials, and a lane-level state machine that hands each
+// lane a new level as soon as it finishes -- its divergent bookkeeping costs
+// more than the idle lanes it saves.)
 __device__ __forceinline__ bool next_unit(const DevBatch& b, int qid, int2& unit) {
     int u = 0;
     if ((threadIdx.x & 31) == 0) u = atomicAdd(&b.hdr->queue[qid], 1);
@@ -54,6 +59,7 @@ __device__ __forceinline__ bool next_unit(const DevBatch& b, int qid, int2& unit
     unit = b.units[u];
     return true;
 }
+
 
 // prepare.cu
 void launch_prepare(const DevBatch& b, cudaStream_t s);
@@ -89,7 +95,6 @@ void launch_gather(const DevBatch& b, int32_t* n_total, int32_t* n_out, double* 
 void launch_newton_df(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_norm_df(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_write_df(const DevBatch& b, int sm_count, cudaStream_t s);
-void launch_twist_df(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_scale_psi(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_twist64(const DevBatch& b, int sm_count, cudaStream_t s);
 
@@ -98,6 +103,7 @@ void launch_refine_long(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_fallback_long(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_norm_long(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_write_long(const DevBatch& b, int sm_count, cudaStream_t s);
+void launch_twist_long(const DevBatch& b, int sm_count, cudaStream_t s);
 
 // adjoint.cu
 void launch_adjoint(const DevBatch& b, const double* dL_dE, double* dL_dV, int64_t total_points,

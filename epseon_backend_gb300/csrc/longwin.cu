@@ -157,9 +157,24 @@ struct LongSide {
     int peak_L, peak_i;
 };
 
+// The twist-index search (MODE 4: outward sweep storing the sampled ratios,
+// MODE 5: inward sweep forming |gamma_k| at the same samples) reuses the
+// state-only chunked march; this is its scratch and result.
+struct TwistIO {
+    double* rho;        // sampled outward ratios (one every kTwistSample points from j0)
+    const double* W;    // a V (FP64) of the potential
+    double aEd;         // a E in FP64
+    int j0, j1, stride;
+    double best;        // MODE 5 result: min |gamma_k| over the samples
+    int k;              //   and its point
+};
+
 template <int MODE>
 __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int from, int to, int dir,
-                                    double* __restrict__ out, double L, int Xk, LongShared& sh) {
+                                    double* __restrict__ out, double L, int Xk, LongShared& sh,
+                                    TwistIO* tw = nullptr) {
+    // MODE 0: state, 1: + sums/peak, 2: + psi write, 4/5: twist sweeps (state)
+    constexpr bool kPsi = MODE == 1 || MODE == 2;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nsteps = (to - from) * dir;
     LongSide<MODE> res;
@@ -185,7 +200,7 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
         int e = 0;
         for (int st = s0; st < s1; ++st) {
             const dfl T = t_of(aE, __ldg(Wf + from + dir * st));
-            if (MODE >= 1) P.v = df_mul(P.v, df_recip(df_add({1.0f, 0.0f}, T)));
+            if (kPsi) P.v = df_mul(P.v, df_recip(df_add({1.0f, 0.0f}, T)));
             df_step(T, A1, D1);
             df_step(T, A2, D2);
             if (((st - s0) & 7) == 7) {
@@ -199,12 +214,12 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
                     D2 = df_scale(D2, sc);
                     e += ee;
                 }
-                if (MODE >= 1) scal_norm(P);
+                if (kPsi) scal_norm(P);
             }
         }
         M = {A1, A2, D1, D2, e};
         mat_norm(M);
-        if (MODE >= 1) scal_norm(P);
+        if (kPsi) scal_norm(P);
     }
 
     // ---- phase 2: exclusive prefix of the transfer matrices (later chunks on the left)
@@ -214,7 +229,7 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
         const Scal py = shfl_up_scal(P, o);
         if (lane >= o) {
             M = mat_mul(M, y);
-            if (MODE >= 1) P = scal_mul(P, py);
+            if (kPsi) P = scal_mul(P, py);
         }
     }
     if (lane == 31) {
@@ -229,7 +244,7 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
             sh.wpre[w] = acc;
             sh.qpre[w] = qa;
             acc = mat_mul(sh.wtot[w], acc);
-            if (MODE >= 1) qa = scal_mul(sh.qtot[w], qa);
+            if (kPsi) qa = scal_mul(sh.qtot[w], qa);
         }
     }
     __syncthreads();
@@ -240,7 +255,7 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
         Px = sh.qpre[warp];
     } else {
         Mx = mat_mul(Mx, sh.wpre[warp]);
-        if (MODE >= 1) Px = scal_mul(Px, sh.qpre[warp]);
+        if (kPsi) Px = scal_mul(Px, sh.qpre[warp]);
     }
 
     // ---- phase 3: this chunk from its starting state (A, D) = Mx (1, 1)
@@ -264,10 +279,31 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
     int peak_L = -(1 << 30), peak_s = 0x7fffffff;
     dfl F = {0.0f, 0.0f};
     if (MODE == 2) F = df_from_double(L * ldexp(1.0, min(1000, max(-1100, eA + eQ - Xk))));
+    double g_best = INFINITY;  // MODE 5
+    int g_k = 0x7fffffff;
     for (int st = s0; st < s1; ++st) {
         const int i = from + dir * st;
         const dfl T = t_of(aE, __ldg(Wf + i));
-        if (MODE >= 1) {
+        if (MODE == 4 || MODE == 5) {
+            // twist search samples, before the step at i: outward, D/A of the
+            // outward state; inward, gamma_i = -12 T_i / f_i + (D/A)_out +
+            // (D/A)_in (the lane twist search's formula)
+            const int rel = i - tw->j0;
+            if (rel % kTwistSample == 0 && rel / kTwistSample < tw->stride) {
+                const double ratio = df_to_double(D) / df_to_double(A);
+                if (MODE == 4) {
+                    tw->rho[rel / kTwistSample] = ratio;
+                } else if (i <= tw->j1 - 1) {
+                    const double Ti = tw->aEd - __ldg(tw->W + i);
+                    const double gam = fabs(-12.0 * Ti / (1.0 + Ti) + tw->rho[rel / kTwistSample] + ratio);
+                    if (gam < g_best || (gam == g_best && i < g_k)) {
+                        g_best = gam;
+                        g_k = i;
+                    }
+                }
+            }
+        }
+        if (kPsi) {
             const dfl f = df_add({1.0f, 0.0f}, T);
             const dfl qn = df_mul(q, df_recip(f));
             const dfl psi = df_mul(A, qn);
@@ -296,7 +332,7 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
                 D = df_scale(D, sc);
                 eA += e;
             }
-            if (MODE >= 1) {
+            if (kPsi) {
                 eq = max(-120, min(120, fexp(q.h)));
                 q = df_scale(q, fpow2(-eq));
                 eQ += eq;
@@ -340,10 +376,25 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
             }
         }
     }
+    if (MODE == 5) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double g2 = __shfl_xor_sync(0xffffffffu, g_best, o);
+            const int k2 = __shfl_xor_sync(0xffffffffu, g_k, o);
+            if (g2 < g_best || (g2 == g_best && k2 < g_k)) {
+                g_best = g2;
+                g_k = k2;
+            }
+        }
+        if (lane == 0) {
+            sh.S[warp] = g_best;
+            sh.pk_s[warp] = g_k;
+        }
+    }
     if (lane == 0) {
         sh.nodes[warp] = nodes;
+        if (MODE != 5) sh.pk_s[warp] = peak_s;
         sh.pk_L[warp] = peak_L;
-        sh.pk_s[warp] = peak_s;
     }
     __syncthreads();
     res.A = sh.A;
@@ -377,6 +428,17 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
     res.S = Ssum;
     res.peak_L = pL;
     res.peak_i = ps == 0x7fffffff ? from : from + dir * ps;
+    if (MODE == 5) {
+        double gb = INFINITY;
+        int gk = 0x7fffffff;
+        for (int w = 0; w < kLongWarps; ++w)
+            if (sh.S[w] < gb || (sh.S[w] == gb && sh.pk_s[w] < gk)) {
+                gb = sh.S[w];
+                gk = sh.pk_s[w];
+            }
+        tw->best = gb;
+        tw->k = gk;
+    }
     __syncthreads();  // the shared scratch is reused by the next call
     return res;
 }
@@ -452,6 +514,9 @@ __global__ void __launch_bounds__(kLongThreads) refine_long_kernel(DevBatch b, i
         }
         int k = clamp_k(w, match_index(m, b.Msuf, E));
         bool done = false, moved_last = false;
+        // (State-only passes reusing an earlier sum as the Newton denominator
+        // are ~40% cheaper each but measured slower overall: more iterations,
+        // and some levels did not converge.)
         int it = 0;
         for (; it < 96; ++it) {
             const PassDF r = long_pass<1>(m, w, Wf, W, E, k, 1.0, sh);
@@ -545,6 +610,58 @@ __global__ void __launch_bounds__(kLongThreads) norm_long_kernel(DevBatch b) {
     }
 }
 
+// Twist-index search for the levels the norm passes flagged (any window
+// length): a chunked outward sweep stores D/A every kTwistSample points, a
+// chunked inward sweep forms |gamma_k| at the same points, the match point
+// becomes argmin |gamma_k| (Dhillon and Parlett's twisted-factorisation
+// rule), then Newton and the norm pass run there.  The level joins the long
+// list, so write_long writes its psi.
+__global__ void __launch_bounds__(kLongThreads) twist_long_kernel(DevBatch b) {
+    __shared__ LongShared sh;
+    const int n = min(b.hdr->n_twist, b.max_twist);
+    for (int q = blockIdx.x; q < n; q += gridDim.x) {
+        const int slot = b.twist_list[q];
+        LevelWork w = b.levels[slot];
+        const PotMeta m = b.meta[w.p];
+        const float2* Wf = b.Wf2 + m.offf;
+        const double* W = b.W64 + m.off;
+        const dfl aE = energy_df(m, w.E);
+        TwistIO tw;
+        tw.rho = b.twist_scratch + (int64_t)q * b.twist_stride;
+        tw.W = W;
+        tw.aEd = __dmul_rn(m.a, w.E);
+        tw.j0 = w.j0;
+        tw.j1 = w.j1;
+        tw.stride = b.twist_stride;
+        tw.best = INFINITY;
+        tw.k = w.k;
+        long_side<4>(Wf, aE, w.j0, w.j1, +1, nullptr, 0.0, 0, sh, &tw);
+        long_side<5>(Wf, aE, w.j1, w.j0, -1, nullptr, 0.0, 0, sh, &tw);
+        const int k = clamp_k(w, tw.k == 0x7fffffff ? w.k : tw.k);
+        double E1 = w.E;
+        PassDF r = long_pass<1>(m, w, Wf, W, E1, k, 1.0, sh);
+        for (int it = 0; it < 8; ++it) {
+            if (r.nodes != w.v || !isfinite(r.dE) || !(fabs(r.dE) < 1e-7)) break;
+            if (fabs(r.dE) <= 1e-13 * fmax(1.0, fabs(E1))) break;
+            E1 += r.dE;
+            r = long_pass<1>(m, w, Wf, W, E1, k, 1.0, sh);
+        }
+        w.E = E1;
+        finalize_df(m, w, r, k);
+        if (threadIdx.x == 0) {
+            if (!(w.status & EPSCU_STATUS_LONG) && b.long_list) {
+                const int t = atomicAdd(&b.hdr->n_long, 1);
+                if (t < b.max_levels) {
+                    b.long_list[t] = slot;
+                    w.status |= EPSCU_STATUS_LONG;
+                }
+            }
+            b.levels[slot] = w;
+        }
+        __syncthreads();
+    }
+}
+
 __global__ void __launch_bounds__(kLongThreads) write_long_kernel(DevBatch b) {
     __shared__ LongShared sh;
     if (!b.psi || b.hdr->error) return;
@@ -581,6 +698,10 @@ void launch_fallback_long(const DevBatch& b, int sm_count, cudaStream_t s) {
 void launch_norm_long(const DevBatch& b, int sm_count, cudaStream_t s) {
     if (!b.long_list) return;
     norm_long_kernel<<<sm_count * 2, kLongThreads, 0, s>>>(b);
+}
+void launch_twist_long(const DevBatch& b, int sm_count, cudaStream_t s) {
+    if (!b.twist_list || !b.long_list) return;
+    twist_long_kernel<<<sm_count * 2, kLongThreads, 0, s>>>(b);
 }
 void launch_write_long(const DevBatch& b, int sm_count, cudaStream_t s) {
     if (!b.long_list) return;

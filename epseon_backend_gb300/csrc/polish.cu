@@ -17,7 +17,8 @@
 //              write; with psi requested its final pass also stores the
 //              unnormalised psi-hat in the level's row, and
 //  scale_psi : applies the constants (one HBM pass over the rows).
-//  twist_df  : twist-index match point for the levels norm_df flagged.
+//  (the twist-index search for the levels norm_df flags is twist_long in
+//  longwin.cu, one CTA per level)
 //  write_df  : recomputes psi from the stored constants (the adjoint's
 //              recompute path).
 #include <cuda_runtime.h>
@@ -288,95 +289,6 @@ __global__ void __launch_bounds__(kThreads, 4) norm_df_kernel(DevBatch b) {
     }
 }
 
-// Twist-index search for the levels norm_df flagged: one full outward sweep
-// samples u_{k-1}/u_k every kTwistSample points, one full inward sweep forms
-// gamma_k at the same points, and the match point becomes argmin |gamma_k|
-// (at an eigenvalue |gamma_k| is smallest where the eigenvector is largest;
-// the rule of Dhillon and Parlett's twisted factorisations).  Then Newton
-// and the norm pass are redone there.
-__global__ void __launch_bounds__(64) twist_df_kernel(DevBatch b) {
-    const int n = min(b.hdr->n_twist, b.max_twist);
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-        const int slot = b.twist_list[q];
-        LevelWork w = b.levels[slot];
-        const PotMeta m = b.meta[w.p];
-        const float2* Wf = b.Wf2 + m.offf;
-        const double* W = b.W64 + m.off;
-        double* rho = b.twist_scratch + (int64_t)q * b.twist_stride;
-        const dfl aE = energy_df(m, w.E);
-        const double aEd = __dmul_rn(m.a, w.E);
-        // outward: before point i the state is ~ (u_i, u_i - u_{i-1})
-        dfl A = {1.0f, 0.0f}, D = {1.0f, 0.0f};
-        for (int i = w.j0; i < w.j1; ++i) {
-            const int j = (i - w.j0) / kTwistSample;
-            if ((i - w.j0) % kTwistSample == 0 && j < b.twist_stride) rho[j] = df_to_double(D) / df_to_double(A);
-            const float2 wv = __ldg(Wf + i);
-            dfl T = two_sum(aE.h, -wv.x);
-            T = fast_two_sum(T.h, __fadd_rn(T.l, __fsub_rn(aE.l, wv.y)));
-            const dfl X = df_add(D, df_mulf(A, -12.0f));
-            D = df_add(D, df_mul(T, X));
-            A = df_add(A, df_add(df_mul(T, A), D));
-            if (((i - w.j0) & 7) == 7) {
-                const float mm = fmaxf(fabsf(A.h), fabsf(D.h));
-                if (mm > 0.0f && mm < INFINITY) {
-                    const float sc = fpow2(-max(-120, min(120, fexp(mm))));
-                    A = df_scale(A, sc);
-                    D = df_scale(D, sc);
-                }
-            }
-        }
-        // inward: before point i the state is ~ (v_i, v_i - v_{i+1})
-        dfl C = {1.0f, 0.0f}, E = {1.0f, 0.0f};
-        double best = INFINITY;
-        int kbest = w.k;
-        for (int i = w.j1; i > w.j0; --i) {
-            if ((i - w.j0) % kTwistSample == 0 && i <= w.j1 - 1) {
-                const int j = (i - w.j0) / kTwistSample;
-                if (j < b.twist_stride) {
-                    const double Ti = aEd - __ldg(W + i);
-                    const double gam = -12.0 * Ti / (1.0 + Ti) + rho[j] + df_to_double(E) / df_to_double(C);
-                    if (fabs(gam) < best) {
-                        best = fabs(gam);
-                        kbest = i;
-                    }
-                }
-            }
-            const float2 wv = __ldg(Wf + i);
-            dfl T = two_sum(aE.h, -wv.x);
-            T = fast_two_sum(T.h, __fadd_rn(T.l, __fsub_rn(aE.l, wv.y)));
-            const dfl X = df_add(E, df_mulf(C, -12.0f));
-            E = df_add(E, df_mul(T, X));
-            C = df_add(C, df_add(df_mul(T, C), E));
-            if (((w.j1 - i) & 7) == 7) {
-                const float mm = fmaxf(fabsf(C.h), fabsf(E.h));
-                if (mm > 0.0f && mm < INFINITY) {
-                    const float sc = fpow2(-max(-120, min(120, fexp(mm))));
-                    C = df_scale(C, sc);
-                    E = df_scale(E, sc);
-                }
-            }
-        }
-        const int k = clamp_k(w, kbest);
-        // Newton at the new match point: the energy was settled at the old one,
-        // so its Cooley correction here may still be above the tolerance
-        double E1 = w.E;
-        double* row = is_long(w) ? nullptr : psi_row(b, m, w);  // long rows: write_long
-        auto pass = [&](double Ep) {
-            return row ? pass_df<3>(m, w, Wf, W, Ep, k, 1.0, row) : pass_df<1>(m, w, Wf, W, Ep, k, 1.0);
-        };
-        PassDF r = pass(E1);
-        for (int it = 0; it < 8; ++it) {
-            if (r.nodes != w.v || !isfinite(r.dE) || !(fabs(r.dE) < 1e-7)) break;
-            if (fabs(r.dE) <= 1e-13 * fmax(1.0, fabs(E1))) break;
-            E1 += r.dE;
-            r = pass(E1);
-        }
-        w.E = E1;
-        finalize_df(m, w, r, k);
-        b.levels[slot] = w;
-    }
-}
-
 __global__ void __launch_bounds__(kThreads, 4) write_df_kernel(DevBatch b) {
     if (!b.psi || b.hdr->error) return;
     const int lane = threadIdx.x & 31;
@@ -455,9 +367,6 @@ void launch_norm_df(const DevBatch& b, int sm_count, cudaStream_t s) {
 }
 void launch_write_df(const DevBatch& b, int sm_count, cudaStream_t s) {
     write_df_kernel<<<sm_count * 8, kThreads, 0, s>>>(b);
-}
-void launch_twist_df(const DevBatch& b, int sm_count, cudaStream_t s) {
-    twist_df_kernel<<<sm_count, 64, 0, s>>>(b);
 }
 
 }  // namespace epscu

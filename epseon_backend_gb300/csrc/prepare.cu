@@ -404,8 +404,9 @@ __device__ int2 decay_window(const PotMeta& m, const DevBatch& b, double Eu, flo
 // Decay window of every level slot (fast method), at E_up = hi0 + 2 delta:
 // an energy above every energy the level's passes use (bracket, Newton steps,
 // the fallback's widened bracket), so one window serves all of them.  Levels
-// whose window is longer than kLongWindow (or kFewWindow in a batch of few
-// levels) go to the long list (CTA-per-level passes).  One warp per level.
+// whose window is longer than the long-window threshold (DevBatch::long_window,
+// else default_long_window of the level count) go to the long list
+// (CTA-per-level passes).  One warp per level.
 // (Sharing one window per warp unit would keep the lanes' loads of W
 // warp-wide broadcasts, but the unit's widest window costs more point-updates
 // than the divergent loads: measured slower on the mixed batch.)
@@ -413,7 +414,8 @@ __global__ void __launch_bounds__(128) window_kernel(DevBatch b, int sm_count) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int n_warps = (gridDim.x * blockDim.x) >> 5;
     const int total = b.hdr->total_levels;
-    const int long_min = total <= kFewLevelsPerSM * sm_count ? kFewWindow : kLongWindow;
+    (void)sm_count;
+    const int long_min = b.long_window > 0 ? b.long_window : default_long_window(total);
     for (int slot = warp; slot < total; slot += n_warps) {
         const LevelWork w = b.levels[slot];
         if (w.status & EPSCU_STATUS_NOTFOUND) continue;

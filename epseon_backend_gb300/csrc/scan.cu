@@ -124,9 +124,18 @@ __device__ __forceinline__ void renorm_f(float& A, float& D) {
     }
 }
 
-// One FP32 difference-form step at a point with W = (w.x + w.y).
-__device__ __forceinline__ void step32(float aEh, float aEl, float2 w, float& A, float& D, int& nodes) {
-    const float T = (aEh - w.x) + (aEl - w.y);
+// The tile in shared memory holds c_i = (H - w.x, -w.y) for the item's
+// reference energy H = a E_mid (one float; the CTA converts each tile once),
+// and a thread's energy enters as l = a E - H, so that
+//     T = a E - W = (H - w.x) + (l - w.y) = c.x + (l + c.y)
+// costs two FADDs per point instead of three.  Near a turning point H and w.x
+// agree to a factor 2 and H - w.x is exact; l spans at most the item's
+// THREADS trial spacings, so its float rounding moves the energy by less than
+// 1e-5 of a spacing.
+
+// One FP32 difference-form step at a point with converted tile entry c.
+__device__ __forceinline__ void step32(float l, float2 c, float& A, float& D, int& nodes) {
+    const float T = c.x + (l + c.y);
     const float X = fmaf(-12.0f, A, D);
     D = fmaf(T, X, D);
     const float inc = fmaf(T, A, D);
@@ -137,8 +146,8 @@ __device__ __forceinline__ void step32(float aEh, float aEl, float2 w, float& A,
 
 // Step with the sign of A shifted into a bit history (one funnel shift per
 // step; the sign changes are popcounted once per 16-step chunk).
-__device__ __forceinline__ void step32b(float aEh, float aEl, float wx, float wy, float& A, float& D, uint32_t& bits) {
-    const float T = (aEh - wx) + (aEl - wy);
+__device__ __forceinline__ void step32b(float l, float cx, float cy, float& A, float& D, uint32_t& bits) {
+    const float T = cx + (l + cy);
     const float X = fmaf(-12.0f, A, D);
     D = fmaf(T, X, D);
     A = A + fmaf(T, A, D);
@@ -151,53 +160,53 @@ __device__ __forceinline__ void flush_bits(uint32_t& bits, int& nodes) {
 }
 
 // 16 ascending points starting at a 16-aligned offset of the tile
-__device__ __forceinline__ void chunk16_up(const float2* __restrict__ c, float aEh, float aEl, float& A, float& D,
+__device__ __forceinline__ void chunk16_up(const float2* __restrict__ c, float l, float& A, float& D,
                                            uint32_t& bits, int& nodes) {
     const float4* q4 = reinterpret_cast<const float4*>(c);
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
         const float4 q = q4[u];
-        step32b(aEh, aEl, q.x, q.y, A, D, bits);
-        step32b(aEh, aEl, q.z, q.w, A, D, bits);
+        step32b(l, q.x, q.y, A, D, bits);
+        step32b(l, q.z, q.w, A, D, bits);
     }
     flush_bits(bits, nodes);
     renorm_f(A, D);
 }
 
 // the same 16 points descending
-__device__ __forceinline__ void chunk16_down(const float2* __restrict__ c, float aEh, float aEl, float& A, float& D,
+__device__ __forceinline__ void chunk16_down(const float2* __restrict__ c, float l, float& A, float& D,
                                              uint32_t& bits, int& nodes) {
     const float4* q4 = reinterpret_cast<const float4*>(c);
 #pragma unroll
     for (int u = 7; u >= 0; --u) {
         const float4 q = q4[u];
-        step32b(aEh, aEl, q.z, q.w, A, D, bits);
-        step32b(aEh, aEl, q.x, q.y, A, D, bits);
+        step32b(l, q.z, q.w, A, D, bits);
+        step32b(l, q.x, q.y, A, D, bits);
     }
     flush_bits(bits, nodes);
     renorm_f(A, D);
 }
 
 // points a0..a1 (a0 <= a1) of tile tb (first point T0), ascending
-__device__ __forceinline__ void run_up(const float2* __restrict__ tb, int T0, int a0, int a1, float aEh, float aEl,
-                                       float& A, float& D, int& nodes) {
+__device__ __forceinline__ void run_up(const float2* __restrict__ tb, int T0, int a0, int a1, float l, float& A,
+                                       float& D, int& nodes) {
     int i = a0;
-    for (; i <= a1 && (i & 15); ++i) step32(aEh, aEl, tb[i - T0], A, D, nodes);
+    for (; i <= a1 && (i & 15); ++i) step32(l, tb[i - T0], A, D, nodes);
     renorm_f(A, D);
     uint32_t bits = __float_as_uint(A) >> 31;
-    for (; i + 15 <= a1; i += 16) chunk16_up(tb + (i - T0), aEh, aEl, A, D, bits, nodes);
-    for (; i <= a1; ++i) step32(aEh, aEl, tb[i - T0], A, D, nodes);
+    for (; i + 15 <= a1; i += 16) chunk16_up(tb + (i - T0), l, A, D, bits, nodes);
+    for (; i <= a1; ++i) step32(l, tb[i - T0], A, D, nodes);
 }
 
 // points a0..a1 (a0 >= a1) of tile tb, descending
-__device__ __forceinline__ void run_down(const float2* __restrict__ tb, int T0, int a0, int a1, float aEh, float aEl,
-                                         float& A, float& D, int& nodes) {
+__device__ __forceinline__ void run_down(const float2* __restrict__ tb, int T0, int a0, int a1, float l, float& A,
+                                         float& D, int& nodes) {
     int i = a0;
-    for (; i >= a1 && ((i & 15) != 15); --i) step32(aEh, aEl, tb[i - T0], A, D, nodes);
+    for (; i >= a1 && ((i & 15) != 15); --i) step32(l, tb[i - T0], A, D, nodes);
     renorm_f(A, D);
     uint32_t bits = __float_as_uint(A) >> 31;
-    for (; i - 15 >= a1; i -= 16) chunk16_down(tb + (i - 15 - T0), aEh, aEl, A, D, bits, nodes);
-    for (; i >= a1; --i) step32(aEh, aEl, tb[i - T0], A, D, nodes);
+    for (; i - 15 >= a1; i -= 16) chunk16_down(tb + (i - 15 - T0), l, A, D, bits, nodes);
+    for (; i >= a1; --i) step32(l, tb[i - T0], A, D, nodes);
 }
 
 template <int THREADS, int TILE, int STAGES>
@@ -276,8 +285,9 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
 
         const double E = trial_energy(m, min(j, b.n_trial - 1));
         const double aE = __dmul_rn(m.a, E);
-        const float aEh = __double2float_rn(aE);
-        const float aEl = __double2float_rn(aE - (double)aEh);
+        // the item's reference energy (middle of its block) and this thread's offset
+        const float H = __double2float_rn(__dmul_rn(m.a, trial_energy(m, min(blk * THREADS + THREADS / 2, b.n_trial - 1))));
+        const float l = __double2float_rn(aE - (double)H);
         const int k = m.k_scan;
         float A = 1.0f, D = 1.0f;  // u_{j0} = 1, u_{j0-1} = 0
         float Ao = 1.0f, Do = 1.0f;
@@ -287,25 +297,35 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
         for (int t = 0; t < L; ++t) {
             const int st = (g_tile + t) % STAGES;
             const uint32_t par = ((g_tile + t) / STAGES) & 1u;
-            if (!mbar_wait_bounded(&full[st], par)) {
+            const bool landed = mbar_wait_bounded(&full[st], par);
+            if (!landed) {
                 atomicExch(&s_abort, 1);
                 atomicCAS(&b.hdr->error, 0, EPSCU_ERR_TIMEOUT);
             }
-            const float2* tb = buf + st * TILE;
-            const int T0 = seq.tile(t) * TILE;
-            if (t < seq.n_out) {
-                const int a0 = max(j0, T0), a1 = min(k - 1, T0 + TILE - 1);
-                run_up(tb, T0, a0, a1, aEh, aEl, A, D, nodes);
-            } else {
-                if (!inward) {
-                    inward = true;
-                    Ao = A;
-                    Do = D;
-                    A = 1.0f;  // v_{j1} = 1, v_{j1+1} = 0
-                    D = 1.0f;
+            float2* tb = buf + st * TILE;
+            // convert the tile: c_i = (H - w.x, -w.y)
+            if (landed)
+                for (int x = tid; x < TILE; x += THREADS) {
+                    const float2 v = tb[x];
+                    tb[x] = make_float2(__fsub_rn(H, v.x), -v.y);
                 }
-                const int a0 = min(j1, T0 + TILE - 1), a1 = max(k + 1, T0);
-                run_down(tb, T0, a0, a1, aEh, aEl, A, D, nodes);
+            __syncthreads();
+            const int T0 = seq.tile(t) * TILE;
+            if (!s_abort) {
+                if (t < seq.n_out) {
+                    const int a0 = max(j0, T0), a1 = min(k - 1, T0 + TILE - 1);
+                    run_up(tb, T0, a0, a1, l, A, D, nodes);
+                } else {
+                    if (!inward) {
+                        inward = true;
+                        Ao = A;
+                        Do = D;
+                        A = 1.0f;  // v_{j1} = 1, v_{j1+1} = 0
+                        D = 1.0f;
+                    }
+                    const int a0 = min(j1, T0 + TILE - 1), a1 = max(k + 1, T0);
+                    run_down(tb, T0, a0, a1, l, A, D, nodes);
+                }
             }
             __syncthreads();  // every thread is done with stage st
             if (s_abort) {

@@ -98,7 +98,9 @@ typedef struct epscu_opts {
                             ordered back to (NULL: the legacy default stream); the work
                             itself runs on the context's stream */
     int32_t tune;        /* 0 = use cached/default launch shape, 1 = autotune */
-    int32_t reserved;
+    int32_t long_window; /* fast method: levels whose window exceeds this many points run
+                            their passes one CTA per level (0: chosen from the number of
+                            levels, 1024 - 16384) */
 } epscu_opts;
 
 /* Caller-owned outputs.  Level slot s of potential p is p*level_capacity + s
