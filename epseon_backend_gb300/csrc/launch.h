@@ -85,7 +85,6 @@ void scan32_set_attributes();
 // levels.cu
 void launch_bisect64(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_refine32(const DevBatch& b, int sm_count, cudaStream_t s);
-void launch_newton64(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_norm64(const DevBatch& b, int use_k, int sm_count, cudaStream_t s);
 void launch_write64(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_gather(const DevBatch& b, int32_t* n_total, int32_t* n_out, double* energy, int32_t* nodes,

@@ -9,7 +9,6 @@
 //             of the scan bracket -- identical arithmetic to the oracle.
 //  refine32 : fast method, safeguarded Cooley-Newton iteration in the FP32
 //             difference form (count + matching residual + norm per pass).
-//  newton64 : fast method, one FP64 Cooley correction from the FP32 energy.
 //  norm64   : FP64 Cooley pass that also fixes the normalisation constants
 //             (sum psi^2 h = 1, psi > 0 next to the inner wall) and the node
 //             count reported for the level.
@@ -150,38 +149,6 @@ __device__ Pass64 cooley64(const PotMeta& m, const double* __restrict__ W, doubl
         r.peak_i = k;
     }
     return r;
-}
-
-// Plain FP64 count pass with the twisted pivot: gamma_k and the stitched
-// node count (no sums), for the Newton step of the fast method.
-__device__ __forceinline__ double gamma64(const PotMeta& m, const double* __restrict__ W, double E, int k, int& nodes) {
-    const double aE = __dmul_rn(m.a, E);
-    double A = 1.0, B = 0.0, C = 1.0, D = 0.0;
-    nodes = 0;
-    int s = 0;
-    for (int i = m.i0; i < k; ++i) {
-        const double Ap = A;
-        step64(aE, __ldg(W + i), A, B);
-        nodes += (A < 0.0) != (Ap < 0.0);
-        if (++s == kRenorm) {
-            s = 0;
-            renorm_pair(A, B);
-        }
-    }
-    s = 0;
-    for (int i = m.i1; i > k; --i) {
-        const double Cp = C;
-        step64(aE, __ldg(W + i), C, D);
-        nodes += (C < 0.0) != (Cp < 0.0);
-        if (++s == kRenorm) {
-            s = 0;
-            renorm_pair(C, D);
-        }
-    }
-    const double Tk = __dsub_rn(aE, __ldg(W + k));
-    const double fk = __dadd_rn(1.0, Tk);
-    const double gk = __fma_rn(-10.0, Tk, 2.0);
-    return gk / fk - B / A - D / C;
 }
 
 // ----------------------------------------------------------------- kernels
@@ -399,53 +366,6 @@ __global__ void __launch_bounds__(kLevelThreads) refine32_kernel(DevBatch b) {
     }
 }
 
-// FP64 Cooley corrections from the FP32 energy at the FP32 match point, with
-// the FP32 sum psi~^2 as the Newton denominator (it only scales the step).
-// One pass is accepted when its step is as small as the FP32 stage allows
-// (quadratic convergence then leaves ~1e-13); otherwise up to three more
-// passes inside an FP64 count bracket, and FP64 bisection on the scan bracket
-// (widened by one trial spacing) as the last resort.
-__global__ void __launch_bounds__(kLevelThreads) newton64_kernel(DevBatch b) {
-    const int total = b.hdr->total_levels;
-    for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < total; slot += gridDim.x * blockDim.x) {
-        LevelWork w = b.levels[slot];
-        if (w.status & (EPSCU_STATUS_NOTFOUND | EPSCU_STATUS_CANCELLED)) continue;
-        const PotMeta m = b.meta[w.p];
-        const double* W = b.W64 + m.off;
-        double E = w.E;
-        double lo64 = w.lo - 1e-8, hi64 = w.hi + 1e-8;
-        bool ok = false;
-        for (int it = 0; it < 4 && !ok; ++it) {
-            int nodes = 0;
-            const double gamma = gamma64(m, W, E, w.k, nodes);
-            const double Tk = __dsub_rn(__dmul_rn(m.a, E), __ldg(W + w.k));
-            const double fk = 1.0 + Tk;
-            const double dE = gamma * fk * fk / (12.0 * m.a * w.norm_k_in);
-            const int count = nodes + (gamma < 0.0 ? 1 : 0);
-            if (count > w.v) hi64 = fmin(hi64, E);
-            else lo64 = fmax(lo64, E);
-            const double En = E + dE;
-            if (!isfinite(En) || !(En >= lo64 && En <= hi64) || nodes != w.v) break;
-            const bool small = fabs(dE) <= (it == 0 ? 1e-8 : 1e-12 * fmax(1.0, fabs(E)));
-            E = En;
-            ok = small;
-        }
-        if (!ok) {
-            const int j = (int)floor((w.E - m.e_lo) / m.delta);
-            double lo = fmax(m.e_lo, m.e_lo + (j - 1) * m.delta), hi = fmin(m.e_cap, m.e_lo + (j + 2) * m.delta);
-            atomicAdd(&b.hdr->fallbacks, 1);
-            for (int itb = 0; itb < m.n_bisect + 3; ++itb) {
-                const double mid = __dmul_rn(0.5, __dadd_rn(lo, hi));
-                if (count64(m, W, mid, w.k) > w.v) hi = mid;
-                else lo = mid;
-            }
-            E = __dmul_rn(0.5, __dadd_rn(lo, hi));
-        }
-        w.E = E;
-        b.levels[slot] = w;
-    }
-}
-
 // Write the normalisation constants of pass r (match point k) into w.
 __device__ __forceinline__ void finalize64(const PotMeta& m, LevelWork& w, const Pass64& r, int k) {
     double ck = 1.0 / sqrt(m.h * r.sum);
@@ -599,9 +519,6 @@ void launch_bisect64(const DevBatch& b, int sm_count, cudaStream_t s) {
 }
 void launch_refine32(const DevBatch& b, int sm_count, cudaStream_t s) {
     refine32_kernel<<<persistent_grid(sm_count, 8), kLevelThreads, 0, s>>>(b);
-}
-void launch_newton64(const DevBatch& b, int sm_count, cudaStream_t s) {
-    newton64_kernel<<<persistent_grid(sm_count, 8), kLevelThreads, 0, s>>>(b);
 }
 void launch_norm64(const DevBatch& b, int use_k, int sm_count, cudaStream_t s) {
     norm64_kernel<<<persistent_grid(sm_count, 8), kLevelThreads, 0, s>>>(b, use_k);
