@@ -275,10 +275,11 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
     int eQ = Px.e;
     int nodes = 0;
     double S = 0.0;
-    dfl Sacc = {0.0f, 0.0f};
+    SqSum ss;
+    ss.init();
     int peak_L = -(1 << 30), peak_s = 0x7fffffff;
     dfl F = {0.0f, 0.0f};
-    if (MODE == 2) F = df_from_double(L * ldexp(1.0, min(1000, max(-1100, eA + eQ - Xk))));
+    if (MODE == 2) F = df_from_double(L * pow2(min(1000, max(-1000, eA + eQ - Xk))));
     double g_best = INFINITY;  // MODE 5
     int g_k = 0x7fffffff;
     for (int st = s0; st < s1; ++st) {
@@ -310,7 +311,7 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
             if (MODE == 1) {
                 const float p = __fmul_rn(psi.h, psi.h);
                 const float e = __fmaf_rn(psi.h, psi.h, -p);
-                Sacc = df_add(Sacc, {p, __fmaf_rn(2.0f * psi.h, psi.l, e)});
+                ss.add({p, __fmaf_rn(2.0f * psi.h, psi.l, e)});
             } else {
                 const dfl v = df_mul(psi, F);
                 out[i] = f2d(v.h) + f2d(v.l);
@@ -337,8 +338,7 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
                 q = df_scale(q, fpow2(-eq));
                 eQ += eq;
                 if (MODE == 1) {
-                    S = (S + (f2d(Sacc.h) + f2d(Sacc.l))) * ldexp(1.0, -2 * (e + eq));
-                    Sacc = {0.0f, 0.0f};
+                    ss.rescale(-2 * (e + eq));
                     const float mag = fabsf(__fmul_rn(A.h, q.h));
                     if (mag > 0.0f) {
                         const int Lm = fexp(mag) + eA + eQ;
@@ -348,11 +348,13 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
                         }
                     }
                 } else if (e + eq != 0) {
-                    F = df_from_double(L * ldexp(1.0, min(1000, max(-1100, eA + eQ - Xk))));
+                    F = df_from_double(L * pow2(min(1000, max(-1000, eA + eQ - Xk))));
                 }
             }
         }
     }
+
+    if (MODE == 1) S = ss.value();
 
     // ---- reductions over the CTA
     const int t_last = (nsteps - 1) / len;
@@ -405,7 +407,7 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
     if (MODE == 1) {
         // this chunk's sum in the side's final scale
         const int d = 2 * (eA + eQ - (res.eA + res.eQ));
-        double term = (s1 > s0 && d > -1000) ? S * ldexp(1.0, min(d, 1000)) : 0.0;
+        double term = (s1 > s0 && d > -1000) ? S * pow2(min(d, 1000)) : 0.0;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) term += __shfl_xor_sync(0xffffffffu, term, o);
         if (lane == 0) sh.S[warp] = term;

@@ -58,10 +58,10 @@ __device__ __forceinline__ void side_df(const float2* __restrict__ Wf, dfl aE, i
     st.S = 0.0;
     st.peak_L = -(1 << 30);
     st.peak_i = from;
-    dfl Sacc = {0.0f, 0.0f};
+    SqSum ss;  // MODE 1/3: sum of psi-hat^2 in the current scale
+    ss.init();
     dfl F = {0.0f, 0.0f};
-    if (MODE == 2) F = df_from_double(L * ldexp(1.0, min(1000, max(-1100, -Xk))));
-    double sc = 1.0;  // MODE 3: 2^(eA + eQ), the absolute scale of psi-hat
+    if (MODE == 2) F = df_from_double(L * pow2(min(1000, max(-1000, -Xk))));
     const int nsteps = (to - from) * dir;
     auto load8 = [&](float2* w8, int base) {
 #pragma unroll
@@ -82,8 +82,13 @@ __device__ __forceinline__ void side_df(const float2* __restrict__ Wf, dfl aE, i
                 if (MODE == 1 || MODE == 3) {
                     const float p = __fmul_rn(psi.h, psi.h);
                     const float e = __fmaf_rn(psi.h, psi.h, -p);
-                    Sacc = df_add(Sacc, {p, __fmaf_rn(2.0f * psi.h, psi.l, e)});
-                    if (MODE == 3) out[i] = (f2d(psi.h) + f2d(psi.l)) * sc;
+                    ss.add({p, __fmaf_rn(2.0f * psi.h, psi.l, e)});
+                    if (MODE == 3) {
+                        // psi-hat in the absolute scale 2^(eA + eQ): exact bit
+                        // constructions and one FP64 add
+                        const int X = max(-900, min(900, st.eA + st.eQ));
+                        out[i] = f2d_pow2(psi.h, X) + f2d_pow2(psi.l, X);
+                    }
                 } else {
                     const dfl v = df_mul(psi, F);
                     out[i] = f2d(v.h) + f2d(v.l);
@@ -111,11 +116,8 @@ __device__ __forceinline__ void side_df(const float2* __restrict__ Wf, dfl aE, i
             eq = max(-120, min(120, fexp(st.q.h)));
             st.q = df_scale(st.q, fpow2(-eq));
             st.eQ += eq;
-            if (MODE == 3 && e + eq != 0) sc = pow2(max(-1000, min(1000, st.eA + st.eQ)));
             if (MODE == 1 || MODE == 3) {
-                // flush the block sum into FP64 in the old scale, then rescale
-                st.S = (st.S + (f2d(Sacc.h) + f2d(Sacc.l))) * ldexp(1.0, -2 * (e + eq));
-                Sacc = {0.0f, 0.0f};
+                ss.rescale(-2 * (e + eq));
                 const float mag = fabsf(__fmul_rn(st.A.h, st.q.h));
                 if (mag > 0.0f) {
                     const int Lm = fexp(mag) + st.eA + st.eQ;
@@ -125,7 +127,7 @@ __device__ __forceinline__ void side_df(const float2* __restrict__ Wf, dfl aE, i
                     }
                 }
             } else if (e + eq != 0) {
-                F = df_from_double(L * ldexp(1.0, min(1000, max(-1100, st.eA + st.eQ - Xk))));
+                F = df_from_double(L * pow2(min(1000, max(-1000, st.eA + st.eQ - Xk))));
             }
         }
         };
@@ -136,7 +138,7 @@ __device__ __forceinline__ void side_df(const float2* __restrict__ Wf, dfl aE, i
         load8(w8, base);
         run8(w8, base);
     }
-    if (MODE == 1 || MODE == 3) st.S += f2d(Sacc.h) + f2d(Sacc.l);
+    if (MODE == 1 || MODE == 3) st.S = ss.value();
 }
 
 // one pass at E with match point k over the level's window [w.j0, w.j1];
