@@ -21,7 +21,7 @@ LEVEL_OK, LEVEL_MAXITER, LEVEL_NONFINITE, LEVEL_UNDER_RESOLVED = 0, 1, 2, 4
 LEVEL_CANCELLED, LEVEL_NOT_FOUND, LEVEL_BAD_INPUT = 8, 16, 32
 METHOD_PLAIN_FP64, METHOD_FAST_FP32C = 0, 1
 KIND_MORSE, KIND_LJ, KIND_SPLINE = 0, 1, 2
-MEM_DEVICE, WANT_PSI, STAGE_TIMING = 1, 2, 4
+MEM_DEVICE, WANT_PSI, STAGE_TIMING, KEEP_PSI = 1, 2, 4, 8
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
@@ -230,7 +230,18 @@ class Solution:
         return self.psi[o : o + n * N].reshape(n, N)
 
 
+class Concatenated(tuple):
+    """(V, offsets, N) of a batch already laid out contiguously (e.g. in pinned
+    memory): passed to Context.solve as is, without a host-side copy."""
+
+    def __new__(cls, V, offsets, N):
+        return super().__new__(cls, (np.ascontiguousarray(V, np.float64), np.asarray(offsets, np.int64),
+                                     np.asarray(N, np.int32)))
+
+
 def concat(Vs):
+    if isinstance(Vs, Concatenated):
+        return Vs
     N = np.array([v.size for v in Vs], np.int32)
     offsets = np.zeros(len(Vs), np.int64)
     offsets[1:] = np.cumsum(N[:-1].astype(np.int64))
@@ -294,10 +305,11 @@ class Context:
         tol: float = 1e-12,
         tune: bool = False,
         long_window: int = 0,
+        keep_psi: bool = False,
     ) -> Solution:
         """Solve a batch of host potentials (host buffers through the C ABI)."""
         V, offsets, N = concat(Vs)
-        n = len(Vs)
+        n = int(N.size)
 
         def arr(x):
             a = np.asarray(x, np.float64)
@@ -333,13 +345,16 @@ class Context:
             _l(psi_off),
             0,
         )
-        o = Opts(int(method), WANT_PSI if want_psi else 0, float(tol), None, 1 if tune else 0, int(long_window))
+        flags = (WANT_PSI if want_psi else 0) | (KEEP_PSI if keep_psi and not want_psi else 0)
+        o = Opts(int(method), flags, float(tol), None, 1 if tune else 0, int(long_window))
         _check(self._lib.epscu_solve(self._h, C.byref(b), C.byref(r), C.byref(o)))
         return Solution(n_total, n_out, energy, nodes, status, err, psi, psi_off, N)
 
-    def adjoint(self, dL_dE: np.ndarray, total_points: int, recompute: bool = False) -> np.ndarray:
+    def adjoint(self, dL_dE: np.ndarray, total_points: int, recompute: bool = False,
+                out: np.ndarray | None = None) -> np.ndarray:
         g = np.ascontiguousarray(dL_dE, np.float64)
-        out = np.zeros(int(total_points))
+        if out is None:
+            out = np.zeros(int(total_points))
         o = Opts(0, 0, 0.0, None, 0, 0)
         _check(self._lib.epscu_adjoint(self._h, _d(g), _d(out), 1 if recompute else 0, C.byref(o)))
         return out
@@ -387,7 +402,7 @@ class DeviceBatch:
 
         self.ctx = ctx
         V, offsets, N = concat(Vs)
-        n = len(Vs)
+        n = int(N.size)
 
         def arr(x):
             a = np.asarray(x, np.float64)

@@ -76,6 +76,7 @@ struct Header {
     unsigned long long scan_updates;    // point-updates the windowed FP32 scan performed
     unsigned long long refine_updates;  // point-updates of the FP32 refinement passes
     unsigned long long df_updates;      // point-updates of the double-float passes
+    long long psi_total;                // psi doubles of the batch (level setup)
 };
 
 // queue ids of the per-level kernels

@@ -65,6 +65,8 @@ struct epscu_ctx {
     int device = 0;
     int sm_count = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;  // the long levels' branch of the fast pipeline
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_zero = nullptr;
     size_t block = size_t(64) << 20;
     std::map<std::string, DevBuf> bufs;
     std::map<std::string, std::pair<void*, size_t>> pinned;
@@ -99,6 +101,10 @@ struct epscu_ctx {
             if (e) cudaEventDestroy(e);
         if (ev_in) cudaEventDestroy(ev_in);
         if (ev_out) cudaEventDestroy(ev_out);
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
+        if (ev_zero) cudaEventDestroy(ev_zero);
+        if (stream2) cudaStreamDestroy(stream2);
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -214,6 +220,7 @@ epscu_status epscu_create(int32_t device_ordinal, epscu_ctx** out) {
     cudaDeviceProp p;
     cudaError_t e = cudaGetDeviceProperties(&p, device_ordinal);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking);
     void* hc = nullptr;
     if (e == cudaSuccess) e = cudaHostAlloc(&hc, 64, cudaHostAllocMapped);
     if (e == cudaSuccess) {
@@ -224,6 +231,9 @@ epscu_status epscu_create(int32_t device_ordinal, epscu_ctx** out) {
     for (int i = 0; i < kStageEvents && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_out, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_zero, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         delete c;
         return fail(EPSCU_ERR_CUDA, std::string("context set-up: ") + cudaGetErrorString(e));
@@ -278,20 +288,25 @@ epscu_status epscu_measure_fma_peaks(epscu_ctx* ctx, double* fp32, double* fp64)
 
 namespace {
 
-// Launch the solve stages of DevBatch b on stream s (capturable).
+// Launch the solve stages of DevBatch b on stream s (capturable).  part 0:
+// everything; 1: up to the level setup (the psi size is then known on the
+// device); 2: the rest.
 void enqueue_pipeline(epscu_ctx* ctx, const DevBatch& b, int method, bool want_psi, const ScanShape& shape,
-                      bool stage_events, cudaStream_t s) {
+                      bool stage_events, cudaStream_t s, int part = 0) {
     auto rec = [&](int i) {
         if (stage_events) cudaEventRecord(ctx->ev[i], s);
     };
-    rec(0);
-    launch_prepare(b, s);
-    if (method == EPSCU_METHOD_FAST_FP32C) launch_scan_window(b, ctx->sm_count, s);  // timed with prepare
-    rec(1);
-    if (method == EPSCU_METHOD_PLAIN_FP64) launch_scan64(b, s);
-    else launch_scan32(b, shape, ctx->sm_count, s);
-    rec(2);
-    launch_level_setup(b, s);
+    if (part != 2) {
+        rec(0);
+        launch_prepare(b, s);
+        if (method == EPSCU_METHOD_FAST_FP32C) launch_scan_window(b, ctx->sm_count, s);  // timed with prepare
+        rec(1);
+        if (method == EPSCU_METHOD_PLAIN_FP64) launch_scan64(b, s);
+        else launch_scan32(b, shape, ctx->sm_count, s);
+        rec(2);
+        launch_level_setup(b, s);
+        if (part == 1) return;
+    }
     if (method == EPSCU_METHOD_PLAIN_FP64) {
         launch_bisect64(b, ctx->sm_count, s);
         rec(3);
@@ -301,14 +316,38 @@ void enqueue_pipeline(epscu_ctx* ctx, const DevBatch& b, int method, bool want_p
         if (want_psi) launch_write64(b, ctx->sm_count, s);
     } else {
         launch_window(b, ctx->sm_count, s);
-        launch_refine32(b, ctx->sm_count, s);
-        launch_refine_long(b, ctx->sm_count, s);
-        rec(3);
-        launch_newton_df(b, ctx->sm_count, s);
-        launch_fallback_long(b, ctx->sm_count, s);
-        launch_norm_df(b, ctx->sm_count, s);
-        launch_norm_long(b, ctx->sm_count, s);
-        launch_twist_long(b, ctx->sm_count, s);
+        if (!stage_events) {
+            // the long levels (one CTA each) and the lane levels are disjoint:
+            // the two branches run side by side, the CTA branch filling the SMs
+            // the lane kernels leave idle as their warps drain
+            // (the psi rows are zeroed there too, an HBM stream beside the
+            // compute-bound refinement, before norm_df writes into them)
+            cudaEventRecord(ctx->ev_fork, s);
+            cudaStreamWaitEvent(ctx->stream2, ctx->ev_fork, 0);
+            launch_refine32(b, ctx->sm_count, s);
+            if (want_psi) launch_zero_psi(b, ctx->sm_count, ctx->stream2);
+            cudaEventRecord(ctx->ev_zero, ctx->stream2);
+            launch_refine_long(b, ctx->sm_count, ctx->stream2);
+            launch_norm_long(b, ctx->sm_count, ctx->stream2);
+            cudaEventRecord(ctx->ev_join, ctx->stream2);
+            launch_newton_df(b, ctx->sm_count, s);
+            launch_fallback_long(b, ctx->sm_count, s);
+            cudaStreamWaitEvent(s, ctx->ev_zero, 0);
+            launch_norm_df(b, ctx->sm_count, s);
+            cudaStreamWaitEvent(s, ctx->ev_join, 0);
+            launch_twist_long(b, ctx->sm_count, s);
+        } else {
+            // stage timing: one stream, stages in sequence
+            launch_refine32(b, ctx->sm_count, s);
+            launch_refine_long(b, ctx->sm_count, s);
+            rec(3);
+            launch_newton_df(b, ctx->sm_count, s);
+            launch_fallback_long(b, ctx->sm_count, s);
+            if (want_psi) launch_zero_psi(b, ctx->sm_count, s);
+            launch_norm_df(b, ctx->sm_count, s);
+            launch_norm_long(b, ctx->sm_count, s);
+            launch_twist_long(b, ctx->sm_count, s);
+        }
         rec(4);
         if (want_psi) {
             launch_scale_psi(b, ctx->sm_count, s);  // rows written unnormalised by norm_df
@@ -339,6 +378,9 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     const int method = opts.method;
     const bool dev = (opts.flags & EPSCU_MEM_DEVICE) != 0;
     const bool want_psi = (opts.flags & EPSCU_WANT_PSI) && res->psi && res->psi_capacity > 0;
+    // host buffers, no psi buffer, psi kept in device memory for the adjoint:
+    // the psi size is read back after the level setup, then the rest runs
+    const bool keep_psi = (opts.flags & EPSCU_KEEP_PSI) && !want_psi && !dev;
     const bool stage_events = (opts.flags & EPSCU_STAGE_TIMING) != 0 || !dev;
     if (n <= 0) return fail(EPSCU_ERR_INVALID, "n_potentials must be positive");
     if (cap <= 0) return fail(EPSCU_ERR_INVALID, "level_capacity must be positive");
@@ -533,13 +575,18 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     keybuf_extra = std::to_string(b.long_window);
     const std::string gkey = std::string(keybuf) + "|" + std::to_string(total_points) + "|" + keybuf_extra;
 
-    auto enqueue_all = [&]() -> cudaError_t {
+    auto enqueue_inputs = [&]() -> cudaError_t {
         cudaError_t e;
         if ((e = cudaMemcpyAsync(b.meta, hm, sizeof(PotMeta) * n, cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
         if ((e = cudaMemcpyAsync(b.order, ho, sizeof(int32_t) * n, cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
         if ((e = cudaMemcpyAsync(d_off, hoff, sizeof(int64_t) * n, cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
         if ((e = cudaMemsetAsync(b.hdr, 0, sizeof(Header), s)) != cudaSuccess) return e;
         if (b.Wf2 && (e = cudaMemsetAsync(b.Wf2, 0, sizeof(float2) * total_padded, s)) != cudaSuccess) return e;
+        return cudaSuccess;
+    };
+    auto enqueue_all = [&]() -> cudaError_t {
+        cudaError_t e = enqueue_inputs();
+        if (e != cudaSuccess) return e;
         enqueue_pipeline(ctx, b, method, want_psi, shape, stage_events, s);
         launch_gather(b, o_nt, o_no, o_e, o_nd, o_st, o_err, method == EPSCU_METHOD_FAST_FP32C ? 1 : 0, s);
         if (stage_events) cudaEventRecord(ctx->ev[6], s);
@@ -572,6 +619,19 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
         EPSCU_CU(cudaEventRecord(ctx->ev[0], s));
         EPSCU_CU(cudaGraphLaunch(ctx->graph, s));
         EPSCU_CU(cudaEventRecord(ctx->ev[6], s));
+    } else if (keep_psi) {
+        EPSCU_CU(enqueue_inputs());
+        enqueue_pipeline(ctx, b, method, true, shape, stage_events, s, 1);
+        EPSCU_CU(cudaMemcpyAsync(hh, b.hdr, sizeof(Header), cudaMemcpyDeviceToHost, s));
+        EPSCU_CU(cudaStreamSynchronize(s));
+        const int64_t need = std::max<int64_t>(1, hh->psi_total);
+        b.psi = (double*)ctx->get("psi_keep", sizeof(double) * (size_t)need, &ce);
+        if (!b.psi) return fail(EPSCU_ERR_NOMEM, "device arena (kept psi)");
+        b.psi_capacity = need;
+        enqueue_pipeline(ctx, b, method, true, shape, stage_events, s, 2);
+        launch_gather(b, o_nt, o_no, o_e, o_nd, o_st, o_err, method == EPSCU_METHOD_FAST_FP32C ? 1 : 0, s);
+        if (stage_events) EPSCU_CU(cudaEventRecord(ctx->ev[6], s));
+        EPSCU_CU(cudaGetLastError());
     } else {
         EPSCU_CU(enqueue_all());
     }
@@ -641,13 +701,14 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     st.fallbacks = hh->fallbacks;
     st.twist_searches = hh->n_twist;
     st.norm_redos = hh->n_redo;
-    st.psi_bytes = want_psi ? psi_total * 8 : 0;
+    st.psi_bytes = (want_psi || keep_psi) ? psi_total * 8 : 0;
     // plain: prepare, scan64, level/unit setup, bracket, bisect64, norm64,
     // twist64, gather (+ write64); fast: prepare, scan window, scan32, level/unit
     // setup, bracket, window, refine32, refine_long, newton_df, fallback
     // (refine_long over the fallback list), norm_df, norm_long, twist_long,
-    // gather (+ scale_psi, write_long)
-    st.kernel_launches = method == EPSCU_METHOD_FAST_FP32C ? 16 + (want_psi ? 2 : 0) : 9 + (want_psi ? 1 : 0);
+    // gather (+ zero_psi, scale_psi, write_long)
+    const bool psi_kernels = want_psi || keep_psi;
+    st.kernel_launches = method == EPSCU_METHOD_FAST_FP32C ? 16 + (psi_kernels ? 3 : 0) : 9 + (psi_kernels ? 1 : 0);
     if (method == EPSCU_METHOD_PLAIN_FP64) {
         st.refine_point_updates = 0;
         int64_t bis = 0;
@@ -665,7 +726,7 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     ctx->last = b;
     ctx->have_last = true;
     ctx->last_method = method;
-    ctx->last_psi = want_psi && hh->error == 0;
+    ctx->last_psi = (want_psi || keep_psi) && hh->error == 0;
     ctx->last_offsets_dev = d_off;
     ctx->last_total_points = total_points;
     ctx->last_psi_total = psi_total;
@@ -702,6 +763,7 @@ extern "C" epscu_status epscu_adjoint(epscu_ctx* ctx, const double* dL_dE, doubl
         const int qid = ctx->last_method == EPSCU_METHOD_FAST_FP32C ? kQWriteDF : kQWrite64;
         EPSCU_CU(cudaMemsetAsync(&b.hdr->queue[qid], 0, sizeof(int32_t), s));
         if (ctx->last_method == EPSCU_METHOD_FAST_FP32C) {
+            launch_zero_psi(b, ctx->sm_count, s);  // write_long writes only the windows
             launch_write_df(b, ctx->sm_count, s);
             launch_write_long(b, ctx->sm_count, s);
         } else {

@@ -95,6 +95,7 @@ void launch_newton_df(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_norm_df(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_write_df(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_scale_psi(const DevBatch& b, int sm_count, cudaStream_t s);
+void launch_zero_psi(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_twist64(const DevBatch& b, int sm_count, cudaStream_t s);
 
 // longwin.cu

@@ -673,12 +673,8 @@ __global__ void __launch_bounds__(kLongThreads) write_long_kernel(DevBatch b) {
         const LevelWork w = b.levels[slot];
         const PotMeta m = b.meta[w.p];
         double* out = b.psi + m.psi_off + (int64_t)(w.v - b.min_level) * m.N;
-        const bool none = no_result(w);
-        // zeros outside the window (the whole row without a result), coalesced
-        const int a = none ? m.N : w.j0;
-        for (int i = threadIdx.x; i < a; i += blockDim.x) out[i] = 0.0;
-        if (none) continue;
-        for (int i = w.j1 + 1 + threadIdx.x; i < m.N; i += blockDim.x) out[i] = 0.0;
+        // the rows were zeroed by zero_psi: only the window is written
+        if (no_result(w)) continue;
         const float2* Wf = b.Wf2 + m.offf;
         const dfl aE = energy_df(m, w.E);
         long_side<2>(Wf, aE, w.j0, w.k, +1, out, w.norm_k_out, w.ex_out, sh);

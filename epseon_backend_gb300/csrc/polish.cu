@@ -323,11 +323,21 @@ __global__ void __launch_bounds__(kThreads, 4) write_df_kernel(DevBatch b) {
     }
 }
 
+// Zeros over the batch's psi rows (the first psi_total doubles), run beside
+// the compute-bound refinement kernels so that the write-back only touches
+// the windows (~a fifth of the rows on the mixed batch).
+__global__ void __launch_bounds__(256) zero_psi_kernel(DevBatch b) {
+    if (!b.psi || b.hdr->error) return;
+    const long long n = min(b.hdr->psi_total, (long long)b.psi_capacity);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        b.psi[i] = 0.0;
+}
+
 // The write-back of the fused norm/write: each row holds the unnormalised
 // psi-hat of the final norm pass on [j0, k) and (k, j1]; scale it by the
-// side constants (norm_k 2^-ex), set psi_k = ck and zero the rest of the row.
-// One warp per level, coalesced: HBM-bound (8 B read + 8 B written per window
-// point, 8 B written elsewhere).
+// side constants (norm_k 2^-ex) and set psi_k = ck.  The rest of the row was
+// zeroed by zero_psi.  One warp per level, coalesced: HBM-bound (8 B read +
+// 8 B written per window point).
 __global__ void __launch_bounds__(256) scale_psi_kernel(DevBatch b) {
     if (!b.psi || b.hdr->error) return;
     const int lane = threadIdx.x & 31;
@@ -339,23 +349,19 @@ __global__ void __launch_bounds__(256) scale_psi_kernel(DevBatch b) {
         if (is_long(w)) continue;  // written by write_long
         const PotMeta m = b.meta[w.p];
         double* row = b.psi + m.psi_off + (int64_t)(w.v - b.min_level) * m.N;
-        if (no_result(w)) {
-            for (int i = lane; i < m.N; i += 32) row[i] = 0.0;
-            continue;
-        }
+        if (no_result(w)) continue;
         const double c_out = w.norm_k_out * pow2(max(-1000, min(1000, -w.ex_out)));
         const double c_in = w.norm_k_in * pow2(max(-1000, min(1000, -w.ex_in)));
-        for (int i = lane; i < m.N; i += 32) {
-            double v = 0.0;
-            if (i >= w.j0 && i < w.k) v = row[i] * c_out;
-            else if (i > w.k && i <= w.j1) v = row[i] * c_in;
-            else if (i == w.k) v = w.ck;
-            row[i] = v;
-        }
+        for (int i = w.j0 + lane; i <= w.j1; i += 32)
+            row[i] = i < w.k ? row[i] * c_out : (i > w.k ? row[i] * c_in : w.ck);
     }
 }
 
 }  // namespace
+
+void launch_zero_psi(const DevBatch& b, int sm_count, cudaStream_t s) {
+    zero_psi_kernel<<<sm_count * 8, 256, 0, s>>>(b);
+}
 
 void launch_scale_psi(const DevBatch& b, int sm_count, cudaStream_t s) {
     scale_psi_kernel<<<sm_count * 8, 256, 0, s>>>(b);

@@ -239,6 +239,7 @@ __global__ void __launch_bounds__(1024) level_setup_kernel(DevBatch b) {
     }
     if (threadIdx.x == 0) {
         b.hdr->total_levels = carry_lv;
+        b.hdr->psi_total = carry_ps;
         b.hdr->queue_refine = 0;
         b.hdr->queue_polish = 0;
         if (b.psi && carry_ps > b.psi_capacity) atomicCAS(&b.hdr->error, 0, 5);

@@ -65,7 +65,10 @@ enum { EPSCU_KIND_MORSE = 0, EPSCU_KIND_LJ = 1, EPSCU_KIND_SPLINE = 2 };
 enum {
     EPSCU_MEM_DEVICE = 1,  /* V / params / outputs are device pointers (else host) */
     EPSCU_WANT_PSI = 2,    /* write normalised wavefunctions */
-    EPSCU_STAGE_TIMING = 4 /* record per-stage CUDA events (disables graph replay) */
+    EPSCU_STAGE_TIMING = 4, /* record per-stage CUDA events (disables graph replay) */
+    EPSCU_KEEP_PSI = 8      /* host buffers without a psi buffer: keep the normalised
+                               wavefunctions in device memory for epscu_adjoint (no
+                               recompute, nothing copied back) */
 };
 
 typedef struct epscu_ctx epscu_ctx;
@@ -92,7 +95,7 @@ typedef struct epscu_batch {
 
 typedef struct epscu_opts {
     int32_t method;      /* EPSCU_METHOD_* */
-    int32_t flags;       /* EPSCU_MEM_DEVICE | EPSCU_WANT_PSI */
+    int32_t flags;       /* EPSCU_MEM_DEVICE | EPSCU_WANT_PSI | EPSCU_STAGE_TIMING | EPSCU_KEEP_PSI */
     double tol;          /* bisection width of the plain method (default 1e-12) */
     void* stream;        /* cudaStream_t the inputs are ordered on and the outputs are
                             ordered back to (NULL: the legacy default stream); the work
@@ -164,8 +167,8 @@ epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, epscu_result*
 
 /* Hellmann-Feynman adjoint of the last solve on this context:
  * dL_dV[offsets[p] + i] = sum_s dL_dE[p*cap + s] * psi_s(r_i)^2 h.
- * Uses the stored wavefunctions of the last solve (EPSCU_WANT_PSI) or
- * recomputes them when recompute != 0.  Pointers follow opts->flags
+ * Uses the wavefunctions the last solve wrote (EPSCU_WANT_PSI) or kept in
+ * device memory (EPSCU_KEEP_PSI), or recomputes them when recompute != 0.  Pointers follow opts->flags
  * (EPSCU_MEM_DEVICE).  No reference counterpart: the reference has no
  * gradients. */
 epscu_status epscu_adjoint(epscu_ctx* ctx, const double* dL_dE, double* dL_dV, int32_t recompute,

@@ -152,6 +152,13 @@ def test_adjoint_recompute_equals_stored(ctx, method):
     scale = np.abs(g_stored).max()
     assert np.max(np.abs(g_recomp - g_stored)) <= 1e-12 * scale
     assert np.array_equal(g_recomp, g_again)
+    # psi kept in device memory by a host-buffer solve (EPSCU_KEEP_PSI): the
+    # adjoint needs no recompute and equals the one on the returned psi
+    s3 = ctx.solve(capi.Concatenated(*capi.concat(Vs)), b.r_min, b.r_max, b.mu, b.e_cap, b.n_trial, method=method,
+                   level_capacity=cap, keep_psi=True)
+    assert np.array_equal(np.nan_to_num(s1.energy), np.nan_to_num(s3.energy))
+    g_kept = ctx.adjoint(gE, total, recompute=False)
+    assert np.max(np.abs(g_kept - g_stored)) <= 1e-12 * scale
 
 
 @pytest.mark.parametrize("method", [capi.METHOD_PLAIN_FP64, capi.METHOD_FAST_FP32C])
