@@ -504,7 +504,7 @@ __global__ void gather_kernel(DevBatch b, int32_t* n_total, int32_t* n_out, doub
         } else {
             energy[o] = NAN;
             nodes[o] = -1;
-            status[o] = EPSCU_STATUS_NOTFOUND | (m.status & EPSCU_STATUS_BAD);
+            status[o] = EPSCU_STATUS_NOTFOUND | (m.status & (EPSCU_STATUS_BAD | EPSCU_STATUS_NONFINITE));
             if (err_est) err_est[o] = NAN;
         }
     }
