@@ -453,7 +453,9 @@ def main():
         "stages_ms": {"prepare": st.ms_prepare, "scan32": st.ms_scan, "refine32": st.ms_refine32,
                       "polish64": st.ms_polish64, "write64": st.ms_write, "solve_total": st.ms_total,
                       "fallbacks": st.fallbacks, "twist_searches": st.twist_searches,
-                      "norm_redos": st.norm_redos},
+                      "norm_redos": st.norm_redos, "refine_max_iters": st.refine_max_iters,
+                      "refine_max_level_updates": st.refine_max_level_updates,
+                      "df_max_level_updates": st.df_max_level_updates},
         "roofline": roof,
         "roofline_plain_fp64": roof_plain,
         "stage_rates": stage_rates,

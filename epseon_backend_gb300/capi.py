@@ -109,6 +109,10 @@ class Stats(C.Structure):
         ("fallbacks", C.c_int32),
         ("twist_searches", C.c_int32),
         ("norm_redos", C.c_int32),
+        ("refine_max_level_updates", C.c_int64),
+        ("df_max_level_updates", C.c_int64),
+        ("refine_max_iters", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 

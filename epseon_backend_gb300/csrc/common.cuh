@@ -57,7 +57,8 @@ struct LevelWork {
     int32_t iters;
     int32_t j0, j1;     // grid window of the level's passes ([i0, i1] unless narrowed
                         // by the decay window of the fast method)
-    int32_t pad0, pad1;
+    int32_t n_in_bracket;  // levels the scan counted inside the scan bracket
+    int32_t pad1;
 };
 
 // Global counters and flags of one solve (device memory).
@@ -77,6 +78,10 @@ struct Header {
     unsigned long long refine_updates;  // point-updates of the FP32 refinement passes
     unsigned long long df_updates;      // point-updates of the double-float passes
     long long psi_total;                // psi doubles of the batch (level setup)
+    unsigned long long refine_max_updates;  // largest per-level point-updates of refine32
+    unsigned long long df_max_updates;      // largest per-level point-updates of newton_df / norm_df
+    int32_t refine_max_iters;               // most refine32 passes of one level
+    int32_t pad_hdr;
 };
 
 // queue ids of the per-level kernels

@@ -6,6 +6,7 @@
 
 #include "common.cuh"
 #include "dfloat.cuh"
+#include "launch.h"
 
 namespace epscu {
 
@@ -76,6 +77,13 @@ __device__ __forceinline__ bool suspicious(const PotMeta& m, const LevelWork& w,
 // whose Cooley correction is above this is redone once at E + dE
 __device__ __forceinline__ bool redo_norm(const LevelWork& w, const PassDF& r) {
     return r.nodes == w.v && isfinite(r.dE) && fabs(r.dE) > 1e-13 * fmax(1.0, fabs(w.E)) && fabs(r.dE) < 1e-8;
+}
+
+// the level's psi row for the fused norm/write, or nullptr (no psi requested,
+// or the psi buffer overflowed: the level setup raised the capacity error)
+__device__ __forceinline__ double* psi_row(const DevBatch& b, const PotMeta& m, const LevelWork& w) {
+    if (!b.psi || b.hdr->error) return nullptr;
+    return b.psi + m.psi_off + (int64_t)(w.v - b.min_level) * m.N;
 }
 
 __device__ __forceinline__ bool no_result(const LevelWork& w) {

@@ -6,11 +6,14 @@
 // the autotune cache of the scan kernel and a CUDA graph of the last
 // device-resident solve (replayed when the same buffers are solved again).
 //
-// Solve pipeline (every stage on the context's stream):
+// Solve pipeline:
 //   prepare -> scan (FP64 | FP32 TMA persistent) -> level set-up + brackets
-//   plain : bisect64 -> norm64 -> write64                      (native FP64)
-//   fast  : refine32 -> newton_df -> norm_df -> write_df       (FP32, then
-//           compensated FP32 with FP64 matching and norm integral)
+//   plain : bisect64 -> norm64 -> twist64 -> write64            (native FP64)
+//   fast  : window, then two branches on two streams (graph fork/join):
+//             lane levels: refine32 -> newton_df -> fallback -> norm_df
+//             long levels: zero_psi -> refine_long -> norm_long
+//           -> twist_long -> scale_psi   (FP32, then compensated FP32 with
+//           FP64 matching and norm integral; the norm passes store psi-hat)
 //   -> gather into the caller's layout.
 #include <cuda_runtime.h>
 
@@ -349,10 +352,8 @@ void enqueue_pipeline(epscu_ctx* ctx, const DevBatch& b, int method, bool want_p
             launch_twist_long(b, ctx->sm_count, s);
         }
         rec(4);
-        if (want_psi) {
-            launch_scale_psi(b, ctx->sm_count, s);  // rows written unnormalised by norm_df
-            launch_write_long(b, ctx->sm_count, s);
-        }
+        // rows written unnormalised by norm_df / norm_long / twist_long
+        if (want_psi) launch_scale_psi(b, ctx->sm_count, s);
     }
     rec(5);
 }
@@ -706,9 +707,9 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     // twist64, gather (+ write64); fast: prepare, scan window, scan32, level/unit
     // setup, bracket, window, refine32, refine_long, newton_df, fallback
     // (refine_long over the fallback list), norm_df, norm_long, twist_long,
-    // gather (+ zero_psi, scale_psi, write_long)
+    // gather (+ zero_psi, scale_psi)
     const bool psi_kernels = want_psi || keep_psi;
-    st.kernel_launches = method == EPSCU_METHOD_FAST_FP32C ? 16 + (psi_kernels ? 3 : 0) : 9 + (psi_kernels ? 1 : 0);
+    st.kernel_launches = method == EPSCU_METHOD_FAST_FP32C ? 16 + (psi_kernels ? 2 : 0) : 9 + (psi_kernels ? 1 : 0);
     if (method == EPSCU_METHOD_PLAIN_FP64) {
         st.refine_point_updates = 0;
         int64_t bis = 0;
@@ -719,6 +720,9 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
         // point-updates: the long-window passes do ~3x this on 256 threads)
         st.refine_point_updates = (int64_t)hh->refine_updates;
         st.fp64_point_updates = (int64_t)hh->df_updates;
+        st.refine_max_level_updates = (int64_t)hh->refine_max_updates;
+        st.df_max_level_updates = (int64_t)hh->df_max_updates;
+        st.refine_max_iters = hh->refine_max_iters;
     }
     ctx->stats = st;
 

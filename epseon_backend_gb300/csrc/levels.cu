@@ -280,9 +280,10 @@ __device__ __forceinline__ Pass32 cooley32(const PotMeta& m, const float2* __res
 // Safeguarded Cooley-Newton in FP32.  The match point follows the peak of
 // |psi| (re-estimated from every pass: matching where the eigenvector is
 // largest keeps the correction quadratic; at a turning point where psi is small
-// it converges to a spurious point).  Every pass updates the count bracket; a
-// small Newton step is confirmed by a count on the far side of the predicted
-// root, otherwise the level continues by bisection.
+// it converges to a spurious point).  Every pass updates the count bracket.  A
+// small Newton step is accepted outright when the scan bracket held this level
+// alone and the pass saw its node count; otherwise it is confirmed by a count
+// on the far side of the predicted root, or the level continues by bisection.
 constexpr double kTol32 = 2e-9;
 
 __global__ void __launch_bounds__(kLevelThreads) refine32_kernel(DevBatch b) {
@@ -342,6 +343,13 @@ __global__ void __launch_bounds__(kLevelThreads) refine32_kernel(DevBatch b) {
                     En = 0.5 * (lo + hi);
                 } else if (fabs(r.dE) <= kTol32) {
                     E_star = En;
+                    if (w.n_in_bracket == 1 && r.nodes == w.v) {
+                        // the scan bracket holds this level alone and the pass
+                        // sees its node count: the root is the level (the
+                        // double-float Newton re-checks the count)
+                        done = true;
+                        break;
+                    }
                     En = En + (r.dE >= 0.0 ? kTol32 : -kTol32);
                     if (En <= lo || En >= hi) En = 0.5 * (E_star + (r.dE >= 0.0 ? hi : lo));
                     confirming = true;
@@ -361,7 +369,10 @@ __global__ void __launch_bounds__(kLevelThreads) refine32_kernel(DevBatch b) {
         w.k = k;
         w.norm_k_in = sum;  // sum psi~^2 at the match point k, the Newton denominator of newton_df
         w.iters = it;
-        atomicAdd(&b.hdr->refine_updates, (unsigned long long)(it + 1) * (unsigned long long)(w.j1 - w.j0));
+        const unsigned long long upd = (unsigned long long)(it + 1) * (unsigned long long)(w.j1 - w.j0);
+        atomicAdd(&b.hdr->refine_updates, upd);
+        atomicMax(&b.hdr->refine_max_updates, upd);
+        atomicMax(&b.hdr->refine_max_iters, it + 1);
         b.levels[slot] = w;
     }
 }

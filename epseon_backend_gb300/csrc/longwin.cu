@@ -173,8 +173,10 @@ template <int MODE>
 __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int from, int to, int dir,
                                     double* __restrict__ out, double L, int Xk, LongShared& sh,
                                     TwistIO* tw = nullptr) {
-    // MODE 0: state, 1: + sums/peak, 2: + psi write, 4/5: twist sweeps (state)
-    constexpr bool kPsi = MODE == 1 || MODE == 2;
+    // MODE 0: state, 1: + sums/peak, 2: + psi write, 3: MODE 1 + unnormalised
+    // psi-hat written in the absolute scale, 4/5: twist sweeps (state)
+    constexpr bool kPsi = MODE == 1 || MODE == 2 || MODE == 3;
+    constexpr bool kSums = MODE == 1 || MODE == 3;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nsteps = (to - from) * dir;
     LongSide<MODE> res;
@@ -308,10 +310,15 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
             const dfl f = df_add({1.0f, 0.0f}, T);
             const dfl qn = df_mul(q, df_recip(f));
             const dfl psi = df_mul(A, qn);
-            if (MODE == 1) {
+            if (kSums) {
                 const float p = __fmul_rn(psi.h, psi.h);
                 const float e = __fmaf_rn(psi.h, psi.h, -p);
                 ss.add({p, __fmaf_rn(2.0f * psi.h, psi.l, e)});
+                if (MODE == 3) {
+                    // psi-hat in the absolute scale 2^(eA + eQ) (as side_df)
+                    const int X = max(-900, min(900, eA + eQ));
+                    out[i] = f2d_pow2(psi.h, X) + f2d_pow2(psi.l, X);
+                }
             } else {
                 const dfl v = df_mul(psi, F);
                 out[i] = f2d(v.h) + f2d(v.l);
@@ -337,7 +344,7 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
                 eq = max(-120, min(120, fexp(q.h)));
                 q = df_scale(q, fpow2(-eq));
                 eQ += eq;
-                if (MODE == 1) {
+                if (kSums) {
                     ss.rescale(-2 * (e + eq));
                     const float mag = fabsf(__fmul_rn(A.h, q.h));
                     if (mag > 0.0f) {
@@ -354,7 +361,7 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
         }
     }
 
-    if (MODE == 1) S = ss.value();
+    if (kSums) S = ss.value();
 
     // ---- reductions over the CTA
     const int t_last = (nsteps - 1) / len;
@@ -367,7 +374,7 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) nodes += __shfl_xor_sync(0xffffffffu, nodes, o);
-    if (MODE == 1) {
+    if (kSums) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             const int L2 = __shfl_xor_sync(0xffffffffu, peak_L, o);
@@ -404,7 +411,7 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
     res.q = sh.q;
     res.eA = sh.eA;
     res.eQ = sh.eQ;
-    if (MODE == 1) {
+    if (kSums) {
         // this chunk's sum in the side's final scale
         const int d = 2 * (eA + eQ - (res.eA + res.eQ));
         double term = (s1 > s0 && d > -1000) ? S * pow2(min(d, 1000)) : 0.0;
@@ -418,7 +425,7 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
     int pL = -(1 << 30), ps = 0x7fffffff;
     for (int w = 0; w < kLongWarps; ++w) {
         nsum += sh.nodes[w];
-        if (MODE == 1) {
+        if (kSums) {
             Ssum += sh.S[w];
             if (sh.pk_L[w] > pL || (sh.pk_L[w] == pL && sh.pk_s[w] < ps)) {
                 pL = sh.pk_L[w];
@@ -446,12 +453,14 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
 }
 
 // One pass at E with match point k (the CTA twin of pass_df<MODE>, MODE 0/1).
+// MODE 3 also stores the unnormalised psi-hat of the window in row.
 template <int MODE>
 __device__ PassDF long_pass(const PotMeta& m, const LevelWork& w, const float2* __restrict__ Wf,
-                            const double* __restrict__ W64, double E, int k, double sum_fallback, LongShared& sh) {
+                            const double* __restrict__ W64, double E, int k, double sum_fallback, LongShared& sh,
+                            double* __restrict__ row = nullptr) {
     const dfl aE = energy_df(m, E);
-    const LongSide<MODE> o = long_side<MODE>(Wf, aE, w.j0, k, +1, nullptr, 0.0, 0, sh);
-    const LongSide<MODE> in = long_side<MODE>(Wf, aE, w.j1, k, -1, nullptr, 0.0, 0, sh);
+    const LongSide<MODE> o = long_side<MODE>(Wf, aE, w.j0, k, +1, row, 0.0, 0, sh);
+    const LongSide<MODE> in = long_side<MODE>(Wf, aE, w.j1, k, -1, row, 0.0, 0, sh);
     const double Tk = __dsub_rn(__dmul_rn(m.a, E), __ldg(W64 + k));
     const double fk = 1.0 + Tk;
     const double Ao = df_to_double(o.A), Do = df_to_double(o.D);
@@ -464,7 +473,7 @@ __device__ PassDF long_pass(const PotMeta& m, const LevelWork& w, const float2* 
     r.peak_log2 = 0;
     r.pk_out = r.pk_in = 0.0;
     r.ex_out = r.ex_in = 0;
-    if (MODE == 1) {
+    if (MODE == 1 || MODE == 3) {
         const double rfk = 1.0 / fk;
         r.pk_out = Ao * df_to_double(o.q) * rfk;
         r.pk_in = Ai * df_to_double(in.q) * rfk;
@@ -483,16 +492,341 @@ __device__ PassDF long_pass(const PotMeta& m, const LevelWork& w, const float2* 
     return r;
 }
 
+// ------------------------------------------------------------------ FP32 passes
+// The CTA-parallel twin of the lane kernel's FP32 Cooley pass (refine32): the
+// same FP32 recurrence and sums, chunked and scanned as above.  It takes a
+// long level from its scan bracket to ~1e-9 at ~1/7 of a double-float pass's
+// cost; the double-float passes then only finish the last digits.
+
+// [[a, b], [c, d]] 2^e in FP32
+struct Mat2f {
+    float a, b, c, d;
+    int e;
+};
+
+struct Scalf {
+    float v;
+    int e;
+};
+
+__device__ __forceinline__ void matf_norm(Mat2f& m) {
+    const float mm = fmaxf(fmaxf(fabsf(m.a), fabsf(m.b)), fmaxf(fabsf(m.c), fabsf(m.d)));
+    if (mm > 0.0f && mm < INFINITY) {
+        const int e = max(-120, min(120, fexp(mm)));
+        const float sc = fpow2(-e);
+        m.a *= sc;
+        m.b *= sc;
+        m.c *= sc;
+        m.d *= sc;
+        m.e += e;
+    }
+}
+
+// x y (x applied after y)
+__device__ __forceinline__ Mat2f matf_mul(const Mat2f& x, const Mat2f& y) {
+    Mat2f r;
+    r.a = fmaf(x.a, y.a, x.b * y.c);
+    r.b = fmaf(x.a, y.b, x.b * y.d);
+    r.c = fmaf(x.c, y.a, x.d * y.c);
+    r.d = fmaf(x.c, y.b, x.d * y.d);
+    r.e = x.e + y.e;
+    matf_norm(r);
+    return r;
+}
+
+__device__ __forceinline__ void scalf_norm(Scalf& s) {
+    const float mm = fabsf(s.v);
+    if (mm > 0.0f && mm < INFINITY) {
+        const int e = max(-120, min(120, fexp(mm)));
+        s.v *= fpow2(-e);
+        s.e += e;
+    }
+}
+
+__device__ __forceinline__ Scalf scalf_mul(const Scalf& x, const Scalf& y) {
+    Scalf r{x.v * y.v, x.e + y.e};
+    scalf_norm(r);
+    return r;
+}
+
+__device__ __forceinline__ Mat2f shfl_up_matf(const Mat2f& m, int o) {
+    return {__shfl_up_sync(0xffffffffu, m.a, o), __shfl_up_sync(0xffffffffu, m.b, o),
+            __shfl_up_sync(0xffffffffu, m.c, o), __shfl_up_sync(0xffffffffu, m.d, o),
+            __shfl_up_sync(0xffffffffu, m.e, o)};
+}
+
+__device__ __forceinline__ Scalf shfl_up_scalf(const Scalf& s, int o) {
+    return {__shfl_up_sync(0xffffffffu, s.v, o), __shfl_up_sync(0xffffffffu, s.e, o)};
+}
+
+struct LongShared32 {
+    Mat2f wtot[kLongWarps], wpre[kLongWarps];
+    Scalf ftot[kLongWarps], fpre[kLongWarps];
+    Scalf fall;  // product of f^2 over the side
+    int nodes[kLongWarps];
+    double S[kLongWarps];
+    int pk_L[kLongWarps], pk_s[kLongWarps];
+    float A, D;  // the side's final state (thread holding the last chunk)
+    int eA;
+};
+
+struct LongSide32 {
+    float A, D;
+    int eA;      // the final state is (A, D) 2^eA
+    int nodes;
+    double S;    // sum_j A_j^2 prod_{l>j} f_l^2 over the side, in units of 2^(2 eA)
+    int peak_L;  // log2 of the largest |A_j| seen at the renormalisations
+    int peak_i;
+};
+
+// One side in FP32 over steps 0..nsteps-1 (point from + dir * step): the
+// state, the node count, the sum S and the peak of |A| exactly as the lane
+// pass accumulates them (S' = f^2 S + A^2 before each step), chunked: phase 1
+// gives each chunk's transfer matrix and product F of f^2, phase 2 scans
+// them, phase 3 re-runs the chunk from its exact start state; a chunk's S is
+// carried to the side's end by the product of F over the later chunks.
+__device__ LongSide32 long_side32(const float2* __restrict__ Wf, float aEh, float aEl, int from, int to, int dir,
+                                  LongShared32& sh) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nsteps = (to - from) * dir;
+    LongSide32 res;
+    if (nsteps <= 0) {
+        res.A = 1.0f;
+        res.D = 1.0f;
+        res.eA = 0;
+        res.nodes = 0;
+        res.S = 0.0;
+        res.peak_L = -(1 << 30);
+        res.peak_i = from;
+        return res;
+    }
+    const int len = (nsteps + kLongThreads - 1) / kLongThreads;
+    const int s0 = min(tid * len, nsteps), s1 = min(s0 + len, nsteps);
+
+    // ---- phase 1: transfer matrix and product of f^2 of this chunk
+    Mat2f M;
+    Scalf F{1.0f, 0};
+    {
+        float A1 = 1.0f, D1 = 0.0f, A2 = 0.0f, D2 = 1.0f;
+        int e = 0;
+        for (int st = s0; st < s1; ++st) {
+            const float2 w = __ldg(Wf + from + dir * st);
+            const float T = (aEh - w.x) + (aEl - w.y);
+            const float f = 1.0f + T;
+            F.v *= f * f;
+            float X = fmaf(-12.0f, A1, D1);
+            D1 = fmaf(T, X, D1);
+            A1 = A1 + fmaf(T, A1, D1);
+            X = fmaf(-12.0f, A2, D2);
+            D2 = fmaf(T, X, D2);
+            A2 = A2 + fmaf(T, A2, D2);
+            if (((st - s0) & 7) == 7) {
+                const float mm = fmaxf(fmaxf(fabsf(A1), fabsf(D1)), fmaxf(fabsf(A2), fabsf(D2)));
+                if (mm > 0.0f && mm < INFINITY) {
+                    const int ee = max(-120, min(120, fexp(mm)));
+                    const float sc = fpow2(-ee);
+                    A1 *= sc;
+                    D1 *= sc;
+                    A2 *= sc;
+                    D2 *= sc;
+                    e += ee;
+                }
+                scalf_norm(F);
+            }
+        }
+        M = {A1, A2, D1, D2, e};
+        matf_norm(M);
+        scalf_norm(F);
+    }
+
+    // ---- phase 2: exclusive prefix of the matrices, inclusive prefix of F
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const Mat2f y = shfl_up_matf(M, o);
+        const Scalf fy = shfl_up_scalf(F, o);
+        if (lane >= o) {
+            M = matf_mul(M, y);
+            F = scalf_mul(F, fy);
+        }
+    }
+    if (lane == 31) {
+        sh.wtot[warp] = M;
+        sh.ftot[warp] = F;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        Mat2f acc = {1.0f, 0.0f, 0.0f, 1.0f, 0};
+        Scalf fa{1.0f, 0};
+        for (int w = 0; w < kLongWarps; ++w) {
+            sh.wpre[w] = acc;
+            sh.fpre[w] = fa;
+            acc = matf_mul(sh.wtot[w], acc);
+            fa = scalf_mul(sh.ftot[w], fa);
+        }
+        sh.fall = fa;
+    }
+    __syncthreads();
+    Mat2f Mx = shfl_up_matf(M, 1);
+    if (lane == 0) Mx = sh.wpre[warp];
+    else Mx = matf_mul(Mx, sh.wpre[warp]);
+    const Scalf Fin = scalf_mul(F, sh.fpre[warp]);  // f^2 over chunks 0..tid
+
+    // ---- phase 3: this chunk from its start state (A, D) = Mx (1, 1)
+    float A = Mx.a + Mx.b, D = Mx.c + Mx.d;
+    int eA = Mx.e;
+    {
+        const float mm = fmaxf(fabsf(A), fabsf(D));
+        if (mm > 0.0f && mm < INFINITY) {
+            const int e = max(-120, min(120, fexp(mm)));
+            const float sc = fpow2(-e);
+            A *= sc;
+            D *= sc;
+            eA += e;
+        }
+    }
+    float S = 0.0f;  // in units of 2^(2 eA)
+    int nodes = 0;
+    int peak_L = -(1 << 30), peak_s = 0x7fffffff;
+    for (int st = s0; st < s1; ++st) {
+        const float2 w = __ldg(Wf + from + dir * st);
+        const float T = (aEh - w.x) + (aEl - w.y);
+        const float f = 1.0f + T;
+        S = fmaf(f * f, S, A * A);
+        const float X = fmaf(-12.0f, A, D);
+        D = fmaf(T, X, D);
+        const float An = A + fmaf(T, A, D);
+        nodes += (__float_as_uint(An) ^ __float_as_uint(A)) >> 31;
+        A = An;
+        if (((st - s0) & 7) == 7 || st == s1 - 1) {
+            const float mm = fmaxf(fabsf(A), fabsf(D));
+            if (mm > 0.0f && mm < INFINITY) {
+                const int e = max(-60, min(60, fexp(mm)));
+                const float sc = fpow2(-e);
+                A *= sc;
+                D *= sc;
+                S *= sc * sc;
+                eA += e;
+            }
+            if (A != 0.0f) {
+                const int L = eA + fexp(fabsf(A));
+                if (L > peak_L) {
+                    peak_L = L;
+                    peak_s = st;
+                }
+            }
+        }
+    }
+
+    // ---- reductions over the CTA
+    const int t_last = (nsteps - 1) / len;
+    if (tid == t_last) {
+        sh.A = A;
+        sh.D = D;
+        sh.eA = eA;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        nodes += __shfl_xor_sync(0xffffffffu, nodes, o);
+        const int L2 = __shfl_xor_sync(0xffffffffu, peak_L, o);
+        const int s2 = __shfl_xor_sync(0xffffffffu, peak_s, o);
+        if (L2 > peak_L || (L2 == peak_L && s2 < peak_s)) {
+            peak_L = L2;
+            peak_s = s2;
+        }
+    }
+    if (lane == 0) {
+        sh.nodes[warp] = nodes;
+        sh.pk_L[warp] = peak_L;
+        sh.pk_s[warp] = peak_s;
+    }
+    __syncthreads();
+    res.A = sh.A;
+    res.D = sh.D;
+    res.eA = sh.eA;
+    {
+        // this chunk's S carried to the side's end (times f^2 over the later
+        // chunks = F_all / F_in) in units of 2^(2 eA_final)
+        double term = 0.0;
+        if (s1 > s0 && S != 0.0f) {
+            const int d = 2 * (eA - res.eA) + sh.fall.e - Fin.e;
+            if (d > -1000) term = (double)S * ((double)sh.fall.v / (double)Fin.v) * pow2(min(d, 1000));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) term += __shfl_xor_sync(0xffffffffu, term, o);
+        if (lane == 0) sh.S[warp] = term;
+    }
+    __syncthreads();
+    int nsum = 0;
+    double Ssum = 0.0;
+    int pL = -(1 << 30), ps = 0x7fffffff;
+    for (int w = 0; w < kLongWarps; ++w) {
+        nsum += sh.nodes[w];
+        Ssum += sh.S[w];
+        if (sh.pk_L[w] > pL || (sh.pk_L[w] == pL && sh.pk_s[w] < ps)) {
+            pL = sh.pk_L[w];
+            ps = sh.pk_s[w];
+        }
+    }
+    res.nodes = nsum;
+    res.S = Ssum;
+    res.peak_L = pL;
+    res.peak_i = ps == 0x7fffffff ? from : from + dir * ps;
+    __syncthreads();  // the shared scratch is reused by the next call
+    return res;
+}
+
+// One FP32 pass at E with match point k (the CTA twin of the lane pass):
+// Cooley correction, count, sum and the peak of |psi| relative to psi_k.
+__device__ PassDF long_pass32(const PotMeta& m, const LevelWork& w, const float2* __restrict__ Wf,
+                              const double* __restrict__ W64, double E, int k, LongShared32& sh) {
+    const double aE = __dmul_rn(m.a, E);
+    const float aEh = __double2float_rn(aE);
+    const float aEl = __double2float_rn(aE - (double)aEh);
+    const LongSide32 o = long_side32(Wf, aEh, aEl, w.j0, k, +1, sh);
+    const LongSide32 in = long_side32(Wf, aEh, aEl, w.j1, k, -1, sh);
+    const double Tk = aE - __ldg(W64 + k);
+    const double fk = 1.0 + Tk;
+    const double uA = o.A, vC = in.A;
+    PassDF r;
+    // gamma_k = -12 T_k / f_k + D_o / u_k + D_i / v_k   (no cancellation)
+    r.gamma = -12.0 * Tk / fk + (double)o.D / uA + (double)in.D / vC;
+    const double fk2 = fk * fk;
+    r.sum = fk2 * (o.S / (uA * uA) + in.S / (vC * vC)) + 1.0;
+    r.dE = r.gamma * fk2 / (12.0 * m.a * r.sum);
+    r.nodes = o.nodes + in.nodes;
+    r.count = r.nodes + (r.gamma < 0.0 ? 1 : 0);
+    const int Lo = o.eA + (o.A != 0.0f ? fexp(fabsf(o.A)) : -1000);
+    const int Li = in.eA + (in.A != 0.0f ? fexp(fabsf(in.A)) : -1000);
+    const int po = o.peak_L - Lo, pi = in.peak_L - Li;
+    r.peak_log2 = max(po, pi);
+    r.peak_i = po >= pi ? o.peak_i : in.peak_i;
+    r.pk_out = r.pk_in = 0.0;
+    r.ex_out = r.ex_in = 0;
+    return r;
+}
+
 __device__ __forceinline__ bool cancelled(const DevBatch& b) { return b.cancel && *b.cancel; }
 
-// Safeguarded Cooley-Newton in double-float from the scan bracket.  Every
-// pass updates the count bracket; Newton steps are taken only while the pass
-// sees the level's own node count (so a neighbouring level cannot attract
-// the iteration) and stay inside the bracket, bisection otherwise.  After the
-// match point moves to the peak of |psi| the pass is redone at the same E.
-// fallback = 0: the long list; 1: the levels newton_df handed over.
+// Long levels from their scan bracket, in three stages:
+//   1. FP32 passes (long_pass32): safeguarded Cooley-Newton to |dE| <= 2e-9
+//      with the count bracket, the match point moved to the peak of |psi|;
+//   2. double-float state-only passes with the FP32 sum as the Newton
+//      denominator (as newton_df): one or two steps to 1e-12;
+//   3. if stage 2 does not settle (the FP32 counts are off near a trial
+//      energy, or the pass sees another node count): safeguarded
+//      Cooley-Newton in double-float with full sums from the scan bracket
+//      widened by one trial spacing.  Every pass updates the count bracket;
+//      Newton steps are taken only while the pass sees the level's own node
+//      count (so a neighbouring level cannot attract the iteration) and stay
+//      inside the bracket, bisection otherwise.  After the match point moves
+//      to the peak of |psi| the pass is redone at the same E.
+// fallback = 0: the long list (stages 1-3); 1: the levels newton_df handed
+// over (stage 3 only).
+constexpr double kTol32Long = 2e-9;
+
 __global__ void __launch_bounds__(kLongThreads) refine_long_kernel(DevBatch b, int fallback) {
     __shared__ LongShared sh;
+    __shared__ LongShared32 sh32;
     const int n = fallback ? min(b.hdr->fallbacks, b.max_levels) : min(b.hdr->n_long, b.max_levels);
     const int32_t* list = fallback ? b.fallback_list : b.long_list;
     for (int q = blockIdx.x; q < n; q += gridDim.x) {
@@ -507,46 +841,96 @@ __global__ void __launch_bounds__(kLongThreads) refine_long_kernel(DevBatch b, i
         const float2* Wf = b.Wf2 + m.offf;
         const double* W = b.W64 + m.off;
         double lo = w.lo, hi = w.hi, E = w.E, sum = 1.0;
-        if (fallback) {
-            // the FP32 bracket may be off by its count errors: restart from
-            // the scan bracket widened by one trial spacing (inside the window)
+        int k = clamp_k(w, match_index(m, b.Msuf, E));
+        bool done = false;
+        int n_pass = 0, n_pass32 = 0;
+        if (!fallback) {
+            // ---- stage 1: FP32
+            bool moved_last = false, ok32 = false;
+            for (int it = 0; it < 48; ++it) {
+                const PassDF r = long_pass32(m, w, Wf, W, E, k, sh32);
+                ++n_pass32;
+                sum = r.sum;
+                if (r.count > w.v) hi = E;
+                else lo = E;
+                if (r.peak_log2 >= 2 && !moved_last) {
+                    k = clamp_k(w, r.peak_i);
+                    moved_last = true;
+                    continue;  // the same energy at the new match point
+                }
+                moved_last = false;
+                const double En = E + r.dE;
+                const bool near = r.nodes == w.v || (m.status & EPSCU_STATUS_UNDER);
+                if (near && isfinite(En) && En > lo && En < hi) {
+                    E = En;
+                    if (fabs(r.dE) <= kTol32Long) {
+                        ok32 = true;
+                        break;
+                    }
+                } else {
+                    E = 0.5 * (lo + hi);
+                }
+                if (hi - lo <= 2.0 * kTol32Long) {
+                    E = 0.5 * (lo + hi);
+                    ok32 = true;
+                    break;
+                }
+            }
+            // ---- stage 2: double-float state-only Newton (FP32 sum)
+            if (ok32) {
+                double lo2 = lo - 1e-8, hi2 = hi + 1e-8;
+                for (int it = 0; it < 4 && !done; ++it) {
+                    const PassDF r = long_pass<0>(m, w, Wf, W, E, k, sum, sh);
+                    ++n_pass;
+                    if (r.count > w.v) hi2 = fmin(hi2, E);
+                    else lo2 = fmax(lo2, E);
+                    const double En = E + r.dE;
+                    if (!isfinite(En) || !(En >= lo2 && En <= hi2) || r.nodes != w.v) break;
+                    done = fabs(r.dE) <= (it == 0 ? 1e-10 : 1e-12 * fmax(1.0, fabs(E)));
+                    E = En;
+                }
+                if (done) {
+                    lo = lo2;
+                    hi = hi2;
+                }
+            }
+        }
+        if (!done) {
+            // ---- stage 3: the FP32 bracket may be off by its count errors:
+            // restart from the scan bracket widened by one trial spacing
             lo = fmax(m.e_lo, w.lo0 - m.delta);
             hi = fmin(m.e_cap, w.hi0 + m.delta);
             if (!(E > lo && E < hi)) E = 0.5 * (lo + hi);
-        }
-        int k = clamp_k(w, match_index(m, b.Msuf, E));
-        bool done = false, moved_last = false;
-        // (State-only passes reusing an earlier sum as the Newton denominator
-        // are ~40% cheaper each but measured slower overall: more iterations,
-        // and some levels did not converge.)
-        int it = 0;
-        for (; it < 96; ++it) {
-            const PassDF r = long_pass<1>(m, w, Wf, W, E, k, 1.0, sh);
-            sum = r.sum;
-            if (r.count > w.v) hi = E;
-            else lo = E;
-            if (r.peak_log2 >= 2 && !moved_last) {
-                k = clamp_k(w, r.peak_i);
-                moved_last = true;
-                continue;  // the same energy at the new match point
-            }
-            moved_last = false;
-            const double tol = 1e-12 * fmax(1.0, fabs(E));
-            const double En = E + r.dE;
-            const bool near = r.nodes == w.v || (m.status & EPSCU_STATUS_UNDER);
-            if (near && isfinite(En) && En > lo && En < hi) {
-                E = En;
-                if (fabs(r.dE) <= tol) {
+            bool moved_last = false;
+            for (int it = 0; it < 96; ++it) {
+                const PassDF r = long_pass<1>(m, w, Wf, W, E, k, 1.0, sh);
+                ++n_pass;
+                sum = r.sum;
+                if (r.count > w.v) hi = E;
+                else lo = E;
+                if (r.peak_log2 >= 2 && !moved_last) {
+                    k = clamp_k(w, r.peak_i);
+                    moved_last = true;
+                    continue;  // the same energy at the new match point
+                }
+                moved_last = false;
+                const double tol = 1e-12 * fmax(1.0, fabs(E));
+                const double En = E + r.dE;
+                const bool near = r.nodes == w.v || (m.status & EPSCU_STATUS_UNDER);
+                if (near && isfinite(En) && En > lo && En < hi) {
+                    E = En;
+                    if (fabs(r.dE) <= tol) {
+                        done = true;
+                        break;
+                    }
+                } else {
+                    E = 0.5 * (lo + hi);
+                }
+                if (hi - lo <= tol) {
+                    E = 0.5 * (lo + hi);
                     done = true;
                     break;
                 }
-            } else {
-                E = 0.5 * (lo + hi);
-            }
-            if (hi - lo <= tol) {
-                E = 0.5 * (lo + hi);
-                done = true;
-                break;
             }
         }
         if (threadIdx.x == 0) {
@@ -557,8 +941,10 @@ __global__ void __launch_bounds__(kLongThreads) refine_long_kernel(DevBatch b, i
             w.E = E;
             w.k = k;
             w.norm_k_in = sum;
-            w.iters = it;
-            atomicAdd(&b.hdr->df_updates, (unsigned long long)(it + 1) * (unsigned long long)(w.j1 - w.j0));
+            w.iters = n_pass32 + n_pass;
+            const unsigned long long pts = (unsigned long long)(w.j1 - w.j0);
+            atomicAdd(&b.hdr->refine_updates, (unsigned long long)n_pass32 * pts);
+            atomicAdd(&b.hdr->df_updates, (unsigned long long)n_pass * pts);
             b.levels[slot] = w;
         }
         __syncthreads();
@@ -566,6 +952,9 @@ __global__ void __launch_bounds__(kLongThreads) refine_long_kernel(DevBatch b, i
 }
 
 // The norm pass of a long level and its match-point candidates (as norm_df).
+// With psi requested every pass also stores its unnormalised psi-hat in the
+// level's row (MODE 3) and the last pass is the one kept; scale_psi applies
+// the constants afterwards.
 __global__ void __launch_bounds__(kLongThreads) norm_long_kernel(DevBatch b) {
     __shared__ LongShared sh;
     const int n = min(b.hdr->n_long, b.max_levels);
@@ -576,20 +965,26 @@ __global__ void __launch_bounds__(kLongThreads) norm_long_kernel(DevBatch b) {
         const PotMeta m = b.meta[w.p];
         const float2* Wf = b.Wf2 + m.offf;
         const double* W = b.W64 + m.off;
+        double* row = psi_row(b, m, w);
+        auto pass = [&](int kk) {
+            return row ? long_pass<3>(m, w, Wf, W, w.E, kk, 1.0, sh, row) : long_pass<1>(m, w, Wf, W, w.E, kk, 1.0, sh);
+        };
         int k = w.k;
-        PassDF r = long_pass<1>(m, w, Wf, W, w.E, k, 1.0, sh);
+        PassDF r = pass(k);
         if (r.peak_log2 >= 2) {
             k = clamp_k(w, r.peak_i);
-            r = long_pass<1>(m, w, Wf, W, w.E, k, 1.0, sh);
+            r = pass(k);
         }
+        int k_row = k;  // the pass whose psi-hat the row holds
         if (r.nodes != w.v) {
             const int kt = clamp_k(w, match_index(m, b.Msuf, w.E));
-            PassDF r2 = long_pass<1>(m, w, Wf, W, w.E, kt, 1.0, sh);
+            PassDF r2 = pass(kt);
             int k2 = kt;
             if (r2.nodes != w.v && r2.peak_log2 >= 1) {
                 k2 = clamp_k(w, r2.peak_i);
-                r2 = long_pass<1>(m, w, Wf, W, w.E, k2, 1.0, sh);
+                r2 = pass(k2);
             }
+            k_row = k2;
             if (r2.nodes == w.v) {
                 r = r2;
                 k = k2;
@@ -598,7 +993,9 @@ __global__ void __launch_bounds__(kLongThreads) norm_long_kernel(DevBatch b) {
         if (redo_norm(w, r)) {
             if (threadIdx.x == 0) atomicAdd(&b.hdr->n_redo, 1);
             w.E += r.dE;
-            r = long_pass<1>(m, w, Wf, W, w.E, k, 1.0, sh);
+            r = pass(k);
+        } else if (row && k_row != k) {
+            r = pass(k);
         }
         finalize_df(m, w, r, k);
         if (threadIdx.x == 0) {
@@ -616,8 +1013,10 @@ __global__ void __launch_bounds__(kLongThreads) norm_long_kernel(DevBatch b) {
 // length): a chunked outward sweep stores D/A every kTwistSample points, a
 // chunked inward sweep forms |gamma_k| at the same points, the match point
 // becomes argmin |gamma_k| (Dhillon and Parlett's twisted-factorisation
-// rule), then Newton and the norm pass run there.  The level joins the long
-// list, so write_long writes its psi.
+// rule), then Newton and the norm pass run there; with psi requested the
+// final pass stores the unnormalised psi-hat in the level's row (scale_psi
+// applies the constants).  The level joins the long list, so the adjoint's
+// recompute path (write_long) writes its psi.
 __global__ void __launch_bounds__(kLongThreads) twist_long_kernel(DevBatch b) {
     __shared__ LongShared sh;
     const int n = min(b.hdr->n_twist, b.max_twist);
@@ -640,13 +1039,17 @@ __global__ void __launch_bounds__(kLongThreads) twist_long_kernel(DevBatch b) {
         long_side<4>(Wf, aE, w.j0, w.j1, +1, nullptr, 0.0, 0, sh, &tw);
         long_side<5>(Wf, aE, w.j1, w.j0, -1, nullptr, 0.0, 0, sh, &tw);
         const int k = clamp_k(w, tw.k == 0x7fffffff ? w.k : tw.k);
+        double* row = psi_row(b, m, w);
+        auto pass = [&](double e) {
+            return row ? long_pass<3>(m, w, Wf, W, e, k, 1.0, sh, row) : long_pass<1>(m, w, Wf, W, e, k, 1.0, sh);
+        };
         double E1 = w.E;
-        PassDF r = long_pass<1>(m, w, Wf, W, E1, k, 1.0, sh);
+        PassDF r = pass(E1);
         for (int it = 0; it < 8; ++it) {
             if (r.nodes != w.v || !isfinite(r.dE) || !(fabs(r.dE) < 1e-7)) break;
             if (fabs(r.dE) <= 1e-13 * fmax(1.0, fabs(E1))) break;
             E1 += r.dE;
-            r = long_pass<1>(m, w, Wf, W, E1, k, 1.0, sh);
+            r = pass(E1);
         }
         w.E = E1;
         finalize_df(m, w, r, k);

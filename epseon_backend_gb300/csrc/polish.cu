@@ -185,13 +185,6 @@ __device__ PassDF pass_df(const PotMeta& m, const LevelWork& w, const float2* __
     return r;
 }
 
-// the level's psi row for the fused norm/write, or nullptr (no psi requested,
-// or the psi buffer overflowed: the level setup raised the capacity error)
-__device__ __forceinline__ double* psi_row(const DevBatch& b, const PotMeta& m, const LevelWork& w) {
-    if (!b.psi || b.hdr->error) return nullptr;
-    return b.psi + m.psi_off + (int64_t)(w.v - b.min_level) * m.N;
-}
-
 __global__ void __launch_bounds__(kThreads, 4) newton_df_kernel(DevBatch b) {
     for (int2 unit; next_unit(b, kQNewtonDF, unit);) {
         if ((int)(threadIdx.x & 31) >= unit.y) continue;
@@ -228,7 +221,11 @@ __global__ void __launch_bounds__(kThreads, 4) newton_df_kernel(DevBatch b) {
         } else {
             w.E = E;
         }
-        atomicAdd(&b.hdr->df_updates, (unsigned long long)n_pass * (unsigned long long)(w.j1 - w.j0));
+        {
+            const unsigned long long upd = (unsigned long long)n_pass * (unsigned long long)(w.j1 - w.j0);
+            atomicAdd(&b.hdr->df_updates, upd);
+            atomicMax(&b.hdr->df_max_updates, upd);
+        }
         b.levels[slot] = w;
     }
 }
@@ -282,7 +279,11 @@ __global__ void __launch_bounds__(kThreads, 4) norm_df_kernel(DevBatch b) {
             r = pass(k);
         }
         finalize_df(m, w, r, k);
-        atomicAdd(&b.hdr->df_updates, (unsigned long long)n_pass * (unsigned long long)(w.j1 - w.j0));
+        {
+            const unsigned long long upd = (unsigned long long)n_pass * (unsigned long long)(w.j1 - w.j0);
+            atomicAdd(&b.hdr->df_updates, upd);
+            atomicMax(&b.hdr->df_max_updates, upd);
+        }
         if (suspicious(m, w, r.nodes, r.dE) && b.twist_list) {
             const int q = atomicAdd(&b.hdr->n_twist, 1);
             if (q < b.max_twist) b.twist_list[q] = slot;
@@ -334,7 +335,8 @@ __global__ void __launch_bounds__(256) zero_psi_kernel(DevBatch b) {
 }
 
 // The write-back of the fused norm/write: each row holds the unnormalised
-// psi-hat of the final norm pass on [j0, k) and (k, j1]; scale it by the
+// psi-hat of the level's final norm pass (norm_df, norm_long or twist_long)
+// on [j0, k) and (k, j1]; scale it by the
 // side constants (norm_k 2^-ex) and set psi_k = ck.  The rest of the row was
 // zeroed by zero_psi.  One warp per level, coalesced: HBM-bound (8 B read +
 // 8 B written per window point).
@@ -346,7 +348,6 @@ __global__ void __launch_bounds__(256) scale_psi_kernel(DevBatch b) {
     const int total = b.hdr->total_levels;
     for (int slot = warp; slot < total; slot += n_warps) {
         const LevelWork w = b.levels[slot];
-        if (is_long(w)) continue;  // written by write_long
         const PotMeta m = b.meta[w.p];
         double* row = b.psi + m.psi_off + (int64_t)(w.v - b.min_level) * m.N;
         if (no_result(w)) continue;

@@ -309,6 +309,7 @@ __global__ void bracket_kernel(DevBatch b) {
         w.dE = 0.0;
         w.norm_k_out = w.norm_k_in = 0.0;
         w.ex_out = w.ex_in = 0;
+        w.n_in_bracket = 0;
         if (lo >= m.n_trial) {
             w.status |= EPSCU_STATUS_NOTFOUND;
             w.lo = w.hi = w.E = m.e_cap;
@@ -316,12 +317,13 @@ __global__ void bracket_kernel(DevBatch b) {
             w.lo = lo == 0 ? m.e_lo : trial_energy(m, lo - 1);
             w.hi = trial_energy(m, lo);
             w.E = __dmul_rn(0.5, __dadd_rn(w.lo, w.hi));
+            w.n_in_bracket = c[lo] - (lo == 0 ? 0 : c[lo - 1]);
         }
         w.lo0 = w.lo;
         w.hi0 = w.hi;
         w.j0 = m.i0;
         w.j1 = m.i1;
-        w.pad0 = w.pad1 = 0;
+        w.pad1 = 0;
         b.levels[m.level_base + s] = w;
     }
 }

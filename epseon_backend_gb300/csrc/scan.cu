@@ -6,15 +6,18 @@
 //           identical to the oracle's eo_count (bit-exact counts).
 //  scan32 : the fast method.  Persistent CTAs pull (potential, energy block)
 //           work items from a device queue, ordered longest grid first.  Each
-//           potential's W = a V is staged into shared memory tile by tile with
-//           1-D bulk TMA copies (cp.async.bulk + mbarrier, STAGES deep) and
-//           read as warp-wide broadcasts.  Each thread carries one trial
+//           potential's W = a V (a float pair per point) is staged into
+//           shared memory tile by tile with 1-D bulk TMA copies
+//           (cp.async.bulk + mbarrier, STAGES deep), converted once per tile
+//           to one float per point relative to the item's reference energy,
+//           and read as warp-wide broadcasts.  Each thread carries one trial
 //           energy through the FP32 difference-form recurrence
 //             D' = D + T (D - 12 A),  A' = A + (T A + D')
-//           (A ~ u_i, D ~ u_i - u_{i-1}; Blatt 1967) with T = aE - W held as an
-//           unevaluated pair of floats, so the count is reliable to
-//           |E - E_v| ~ 1e-9 Hartree.  The twist pivot is evaluated in FP64 in
-//           the cancellation-free form -12 T_k A C + f_k (D_o C + D_i A).
+//           (A ~ u_i, D ~ u_i - u_{i-1}; Blatt 1967) with T = aE - W rounded
+//           once relative to |T| and to the energy offset inside the item, so
+//           the count is reliable to |E - E_v| of a few 1e-9 Hartree.  The
+//           twist pivot is evaluated in FP64 in the cancellation-free form
+//           -12 T_k A C + f_k (D_o C + D_i A).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -124,18 +127,20 @@ __device__ __forceinline__ void renorm_f(float& A, float& D) {
     }
 }
 
-// The tile in shared memory holds c_i = (H - w.x, -w.y) for the item's
-// reference energy H = a E_mid (one float; the CTA converts each tile once),
-// and a thread's energy enters as l = a E - H, so that
-//     T = a E - W = (H - w.x) + (l - w.y) = c.x + (l + c.y)
-// costs two FADDs per point instead of three.  Near a turning point H and w.x
-// agree to a factor 2 and H - w.x is exact; l spans at most the item's
-// THREADS trial spacings, so its float rounding moves the energy by less than
-// 1e-5 of a spacing.
+// Each landed tile of W = w.x + w.y (a float pair per point) is converted
+// once into c_i = (H - w.x) - w.y, one float per point, for the item's
+// reference energy H = a E_mid, and a thread's energy enters as l = a E - H, so
+//     T = a E - W = c_i + l
+// costs one FADD per point.  Rounding: near the turning point of H, H and w.x
+// agree to a factor 2 and H - w.x is exact; c_i then carries one rounding of
+// |H - W|, and T one of |T|.  At a thread's own turning point (T ~ 0,
+// |H - W| ~ |l|) the error is ulp(l)/2 with l at most THREADS trial spacings,
+// the same as keeping W's low part through a second FADD; elsewhere it is at
+// most twice that scheme's ulp(T)/2.
 
 // One FP32 difference-form step at a point with converted tile entry c.
-__device__ __forceinline__ void step32(float l, float2 c, float& A, float& D, int& nodes) {
-    const float T = c.x + (l + c.y);
+__device__ __forceinline__ void step32(float l, float c, float& A, float& D, int& nodes) {
+    const float T = c + l;
     const float X = fmaf(-12.0f, A, D);
     D = fmaf(T, X, D);
     const float inc = fmaf(T, A, D);
@@ -146,8 +151,8 @@ __device__ __forceinline__ void step32(float l, float2 c, float& A, float& D, in
 
 // Step with the sign of A shifted into a bit history (one funnel shift per
 // step; the sign changes are popcounted once per 16-step chunk).
-__device__ __forceinline__ void step32b(float l, float cx, float cy, float& A, float& D, uint32_t& bits) {
-    const float T = cx + (l + cy);
+__device__ __forceinline__ void step32b(float l, float c, float& A, float& D, uint32_t& bits) {
+    const float T = c + l;
     const float X = fmaf(-12.0f, A, D);
     D = fmaf(T, X, D);
     A = A + fmaf(T, A, D);
@@ -160,35 +165,39 @@ __device__ __forceinline__ void flush_bits(uint32_t& bits, int& nodes) {
 }
 
 // 16 ascending points starting at a 16-aligned offset of the tile
-__device__ __forceinline__ void chunk16_up(const float2* __restrict__ c, float l, float& A, float& D,
+__device__ __forceinline__ void chunk16_up(const float* __restrict__ c, float l, float& A, float& D,
                                            uint32_t& bits, int& nodes) {
     const float4* q4 = reinterpret_cast<const float4*>(c);
 #pragma unroll
-    for (int u = 0; u < 8; ++u) {
+    for (int u = 0; u < 4; ++u) {
         const float4 q = q4[u];
-        step32b(l, q.x, q.y, A, D, bits);
-        step32b(l, q.z, q.w, A, D, bits);
+        step32b(l, q.x, A, D, bits);
+        step32b(l, q.y, A, D, bits);
+        step32b(l, q.z, A, D, bits);
+        step32b(l, q.w, A, D, bits);
     }
     flush_bits(bits, nodes);
     renorm_f(A, D);
 }
 
 // the same 16 points descending
-__device__ __forceinline__ void chunk16_down(const float2* __restrict__ c, float l, float& A, float& D,
+__device__ __forceinline__ void chunk16_down(const float* __restrict__ c, float l, float& A, float& D,
                                              uint32_t& bits, int& nodes) {
     const float4* q4 = reinterpret_cast<const float4*>(c);
 #pragma unroll
-    for (int u = 7; u >= 0; --u) {
+    for (int u = 3; u >= 0; --u) {
         const float4 q = q4[u];
-        step32b(l, q.z, q.w, A, D, bits);
-        step32b(l, q.x, q.y, A, D, bits);
+        step32b(l, q.w, A, D, bits);
+        step32b(l, q.z, A, D, bits);
+        step32b(l, q.y, A, D, bits);
+        step32b(l, q.x, A, D, bits);
     }
     flush_bits(bits, nodes);
     renorm_f(A, D);
 }
 
 // points a0..a1 (a0 <= a1) of tile tb (first point T0), ascending
-__device__ __forceinline__ void run_up(const float2* __restrict__ tb, int T0, int a0, int a1, float l, float& A,
+__device__ __forceinline__ void run_up(const float* __restrict__ tb, int T0, int a0, int a1, float l, float& A,
                                        float& D, int& nodes) {
     int i = a0;
     for (; i <= a1 && (i & 15); ++i) step32(l, tb[i - T0], A, D, nodes);
@@ -199,7 +208,7 @@ __device__ __forceinline__ void run_up(const float2* __restrict__ tb, int T0, in
 }
 
 // points a0..a1 (a0 >= a1) of tile tb, descending
-__device__ __forceinline__ void run_down(const float2* __restrict__ tb, int T0, int a0, int a1, float l, float& A,
+__device__ __forceinline__ void run_down(const float* __restrict__ tb, int T0, int a0, int a1, float l, float& A,
                                          float& D, int& nodes) {
     int i = a0;
     for (; i >= a1 && ((i & 15) != 15); --i) step32(l, tb[i - T0], A, D, nodes);
@@ -212,7 +221,8 @@ __device__ __forceinline__ void run_down(const float2* __restrict__ tb, int T0, 
 template <int THREADS, int TILE, int STAGES>
 __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, int n_items) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    float2* buf = reinterpret_cast<float2*>(smem_raw);
+    float2* buf = reinterpret_cast<float2*>(smem_raw);               // STAGES TMA tiles of (w.x, w.y)
+    float* conv = reinterpret_cast<float*>(buf + (size_t)STAGES * TILE);  // the converted tile
     __shared__ __align__(8) uint64_t full[STAGES];
     __shared__ int s_item;
     __shared__ int s_abort;
@@ -302,36 +312,19 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
                 atomicExch(&s_abort, 1);
                 atomicCAS(&b.hdr->error, 0, EPSCU_ERR_TIMEOUT);
             }
-            float2* tb = buf + st * TILE;
-            // convert the tile: c_i = (H - w.x, -w.y)
+            const float2* tb = buf + st * TILE;
+            // convert the tile: c_i = (H - w.x) - w.y
             if (landed)
                 for (int x = tid; x < TILE; x += THREADS) {
                     const float2 v = tb[x];
-                    tb[x] = make_float2(__fsub_rn(H, v.x), -v.y);
+                    conv[x] = __fsub_rn(__fsub_rn(H, v.x), v.y);
                 }
-            __syncthreads();
-            const int T0 = seq.tile(t) * TILE;
-            if (!s_abort) {
-                if (t < seq.n_out) {
-                    const int a0 = max(j0, T0), a1 = min(k - 1, T0 + TILE - 1);
-                    run_up(tb, T0, a0, a1, l, A, D, nodes);
-                } else {
-                    if (!inward) {
-                        inward = true;
-                        Ao = A;
-                        Do = D;
-                        A = 1.0f;  // v_{j1} = 1, v_{j1+1} = 0
-                        D = 1.0f;
-                    }
-                    const int a0 = min(j1, T0 + TILE - 1), a1 = max(k + 1, T0);
-                    run_down(tb, T0, a0, a1, l, A, D, nodes);
-                }
-            }
-            __syncthreads();  // every thread is done with stage st
+            __syncthreads();  // conv is complete, stage st is free
             if (s_abort) {
                 g_tile += t;  // tiles t.. were issued but not consumed
                 break;
             }
+            // refill stage st while the tile is marched
             if (tid == 0 && t + STAGES < L) {
                 fence_proxy_async();
                 mbar_expect_tx(&full[st], TILE * sizeof(float2));
@@ -339,6 +332,22 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
                           &full[st]);
                 ++g_issue;
             }
+            const int T0 = seq.tile(t) * TILE;
+            if (t < seq.n_out) {
+                const int a0 = max(j0, T0), a1 = min(k - 1, T0 + TILE - 1);
+                run_up(conv, T0, a0, a1, l, A, D, nodes);
+            } else {
+                if (!inward) {
+                    inward = true;
+                    Ao = A;
+                    Do = D;
+                    A = 1.0f;  // v_{j1} = 1, v_{j1+1} = 0
+                    D = 1.0f;
+                }
+                const int a0 = min(j1, T0 + TILE - 1), a1 = max(k + 1, T0);
+                run_down(conv, T0, a0, a1, l, A, D, nodes);
+            }
+            __syncthreads();  // every thread is done with conv
         }
         if (s_abort) break;
         g_tile += L;
@@ -368,7 +377,7 @@ template <int THREADS, int TILE, int STAGES>
 void launch_scan32_t(const DevBatch& b, int ctas_per_sm, int sm_count, cudaStream_t s) {
     const int ipp = (b.n_trial + THREADS - 1) / THREADS;
     const int n_items = ipp * b.n;
-    const size_t smem = (size_t)TILE * STAGES * sizeof(float2);
+    const size_t smem = (size_t)TILE * STAGES * sizeof(float2) + (size_t)TILE * sizeof(float);
     auto kern = scan32_kernel<THREADS, TILE, STAGES>;
     if (ctas_per_sm <= 0) {
         int occ = 0;
@@ -384,7 +393,7 @@ void launch_scan32_t(const DevBatch& b, int ctas_per_sm, int sm_count, cudaStrea
 template <int THREADS, int TILE, int STAGES>
 void set_attr_t() {
     cudaFuncSetAttribute(scan32_kernel<THREADS, TILE, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(TILE * STAGES * sizeof(float2)));
+                         (int)(TILE * STAGES * sizeof(float2) + TILE * sizeof(float)));
 }
 
 }  // namespace

@@ -222,6 +222,13 @@ typedef struct epscu_stats {
     int32_t fallbacks;             /* levels that needed the bisection fallback */
     int32_t twist_searches;        /* levels re-matched by the twist-index search */
     int32_t norm_redos;            /* norm passes redone at E + dE (fast method) */
+    int64_t refine_max_level_updates; /* largest point-updates of one level's FP32
+                                         refinement (fast method; the tail of the
+                                         lane kernel) */
+    int64_t df_max_level_updates;  /* largest point-updates of one level's double-float
+                                      passes on the lane path (fast method) */
+    int32_t refine_max_iters;      /* most FP32 refinement passes of one level */
+    int32_t reserved;
 } epscu_stats;
 epscu_status epscu_last_stats(epscu_ctx* ctx, epscu_stats* stats);
 
