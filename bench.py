@@ -242,6 +242,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--batch", type=int, default=None,
                     help="potentials per GPU of the mixed workload (default 2048; smaller for profiler captures)")
+    ap.add_argument("--long-window", type=int, default=0,
+                    help="window length above which a level runs one CTA per level (0: the library's default, "
+                         "chosen from the level count)")
     ap.add_argument("--workload", default="mixed", choices=sorted(WORKLOADS),
                     help="mixed = the headline batch; the others are the single-Morse, 64-Morse, adjoint and "
                          "long-grid cases")
@@ -316,17 +319,17 @@ def main():
     mask = (slot < n_lev[:, None]).to(torch.float64)
 
     def step():
-        db.solve(capi.METHOD_FAST_FP32C, stream=stream.cuda_stream)
+        db.solve(capi.METHOD_FAST_FP32C, long_window=args.long_window, stream=stream.cuda_stream)
         gE = 2.0 * w * (torch.nan_to_num(db.energy) - target) * mask
         db.adjoint(gE, stream=stream.cuda_stream)
 
-    db.solve(capi.METHOD_FAST_FP32C, tune=True, stream=stream.cuda_stream)  # autotune the scan shape
+    db.solve(capi.METHOD_FAST_FP32C, long_window=args.long_window, tune=True, stream=stream.cuda_stream)  # autotune the scan shape
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
 
     # stage timing of one instrumented solve (per-kernel events on the solve stream)
-    db.solve(capi.METHOD_FAST_FP32C, stage_timing=True, stream=stream.cuda_stream)
+    db.solve(capi.METHOD_FAST_FP32C, long_window=args.long_window, stage_timing=True, stream=stream.cuda_stream)
     st = ctx.stats()
     torch.cuda.synchronize()
 
@@ -365,7 +368,7 @@ def main():
 
     def e2e_step():
         sol = ctx.solve(batch_host, b.r_min, b.r_max, b.mu, b.e_cap, b.n_trial, method=capi.METHOD_FAST_FP32C,
-                        level_capacity=cap, keep_psi=True)
+                        level_capacity=cap, keep_psi=True, long_window=args.long_window)
         gEh = 2.0 * w_np * (np.nan_to_num(sol.energy) - target_np) * maskh
         return sol, gEh, ctx.adjoint(gEh, Vcat.size, recompute=False, out=gV_pinned.numpy())
 

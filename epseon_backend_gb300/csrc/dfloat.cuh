@@ -148,6 +148,46 @@ struct SqSum {
     }
 };
 
+// The double of a double-float pair h + l (|l| <= ulp(h)/2, as every
+// operation above leaves it) within one unit in its last place, built with
+// integer operations only: h's significand at the top of the 53 bits, l's
+// added or subtracted below it (its bits past the 53rd are dropped).  Zero,
+// subnormal or non-finite h, and pairs that are not normalised, take two
+// exact conversions and one FP64 add instead.
+__device__ __forceinline__ double df_pair_to_double(float h, float l) {
+    const uint32_t uh = __float_as_uint(h), ul = __float_as_uint(l);
+    const uint32_t eh = (uh >> 23) & 0xffu, el = (ul >> 23) & 0xffu;
+    if (eh == 0u || eh == 0xffu || el == 0xffu) return f2d(h) + f2d(l);
+    uint64_t M = (uint64_t)((uh & 0x7fffffu) | 0x800000u) << 29;  // bits 52..29
+    if (el != 0u) {  // (a subnormal l lies below the 53 bits)
+        const int d = (int)eh - (int)el;
+        if (d < 24) return f2d(h) + f2d(l);
+        const uint64_t ml = (uint64_t)((ul & 0x7fffffu) | 0x800000u);
+        const int sh = 29 - d;  // <= 5: l's significand stays below bit 29
+        const uint64_t add = sh >= 0 ? (ml << sh) : (-sh < 64 ? (ml >> -sh) : 0ull);
+        M = ((uh ^ ul) >> 31) ? M - add : M + add;
+    }
+    uint32_t e = eh + 896u;  // biased double exponent of bit 52
+    if (!(M >> 52)) {        // a subtraction from a power of two: one bit down
+        M <<= 1;
+        --e;
+    }
+    return __longlong_as_double((long long)(((uint64_t)(uh >> 31) << 63) | ((uint64_t)e << 52) |
+                                            (M & 0xfffffffffffffull)));
+}
+
+// df_pair_to_double(h, l) * 2^e2, the exponent added in the bits while the
+// result stays a normal double (ldexp otherwise)
+__device__ __forceinline__ double df_pair_to_double_scaled(float h, float l, int e2) {
+    const double d = df_pair_to_double(h, l);
+    const long long u = __double_as_longlong(d);
+    const int ex = (int)((u >> 52) & 0x7ff);
+    if (ex == 0) return d;  // zero (a subnormal pair product: below any psi value)
+    const int en = ex + e2;
+    if (en >= 1 && en <= 2046) return __longlong_as_double(u + ((long long)e2 << 52));
+    return ldexp(d, e2);
+}
+
 __device__ __forceinline__ dfl df_from_double(double x) {
     const float h = __double2float_rn(x);
     const float l = __double2float_rn(x - (double)h);

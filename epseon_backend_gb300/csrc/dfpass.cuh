@@ -79,6 +79,37 @@ __device__ __forceinline__ bool redo_norm(const LevelWork& w, const PassDF& r) {
     return r.nodes == w.v && isfinite(r.dE) && fabs(r.dE) > 1e-13 * fmax(1.0, fabs(w.E)) && fabs(r.dE) < 1e-8;
 }
 
+// The norm passes store psi-hat = (h + l) 2^X in the 8 bytes of each window
+// point of the level's row as a tagged float pair for scale_psi: X = 64 r + x
+// with x in [-32, 31], the pair (h 2^x, l 2^x) in floats, and r in the five
+// low bits of the second float (which only cost l bits 2^-43 below h).  X can
+// reach hundreds (a window edge deep in a steep wall lies far below the peak);
+// |X| is clamped to the tag's range of about +-1000, beyond any value that
+// survives the normalisation.
+struct PsiTag {
+    float sc;  // 2^x
+    int r;     // the tag
+};
+
+__device__ __forceinline__ PsiTag psi_tag(int X) {
+    X = max(-1000, min(X, 990));
+    const int r = (X + 32) >> 6;  // floor((X + 32) / 64): x = X - 64 r in [-32, 31]
+    return {fpow2(X - 64 * r), r};
+}
+
+__device__ __forceinline__ void store_psi_pair(double* __restrict__ row, int i, dfl psi, PsiTag t) {
+    const float l = __fmul_rn(psi.l, t.sc);
+    const uint32_t lt = (__float_as_uint(l) & ~31u) | ((uint32_t)t.r & 31u);
+    reinterpret_cast<float2*>(row)[i] = make_float2(__fmul_rn(psi.h, t.sc), __uint_as_float(lt));
+}
+
+// the stored pair back: (h, l) and the tag r (psi-hat = (h + l) 2^(64 r))
+__device__ __forceinline__ dfl load_psi_pair(float2 v, int& r) {
+    const uint32_t lt = __float_as_uint(v.y);
+    r = ((int)(lt << 27)) >> 27;  // sign-extended five bits
+    return {v.x, __uint_as_float(lt & ~31u)};
+}
+
 // the level's psi row for the fused norm/write, or nullptr (no psi requested,
 // or the psi buffer overflowed: the level setup raised the capacity error)
 __device__ __forceinline__ double* psi_row(const DevBatch& b, const PotMeta& m, const LevelWork& w) {

@@ -544,8 +544,10 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
         EPSCU_CU(cudaMemsetAsync(b.hdr, 0, sizeof(Header), s));
         launch_prepare(b, s);
         launch_scan_window(b, ctx->sm_count, s);
-        const ScanShape cands[] = {{128, 1024, 4, 0}, {128, 2048, 3, 0}, {256, 1024, 4, 0}, {256, 2048, 3, 0},
-                                   {256, 4096, 2, 0}, {512, 1024, 4, 0}, {512, 2048, 3, 0}};
+        // (fewer stages: less shared memory, more resident CTAs per SM)
+        const ScanShape cands[] = {{128, 1024, 2, 0}, {128, 1024, 4, 0}, {128, 2048, 2, 0}, {128, 2048, 3, 0},
+                                   {256, 1024, 2, 0}, {256, 1024, 4, 0}, {256, 2048, 3, 0}, {256, 4096, 2, 0},
+                                   {512, 1024, 4, 0}, {512, 2048, 3, 0}};
         float best = 1e30f;
         for (const ScanShape& c : cands) {
             EPSCU_CU(cudaMemsetAsync(&b.hdr->queue_scan, 0, sizeof(int32_t), s));

@@ -188,78 +188,105 @@ struct Pass32 {
     int peak_i, peak_log2;
 };
 
+// One side's FP32 state: u ~ A 2^ecum, D ~ u_i - u_{i-dir}, S = sum of A_j^2
+// weighted by the f^2 of the later points (the Cooley denominator), node
+// count and the peak of |A| seen at the renormalisations.
+struct Side32 {
+    float A, D, S;
+    int ecum, nodes, Lpk, ipk;
+};
+
+__device__ __forceinline__ void step32s(Side32& s, float aEh, float aEl, float2 w) {
+    const float T = (aEh - w.x) + (aEl - w.y);
+    const float f = 1.0f + T;
+    s.S = fmaf(f * f, s.S, s.A * s.A);
+    const float X = fmaf(-12.0f, s.A, s.D);
+    s.D = fmaf(T, X, s.D);
+    const float An = s.A + fmaf(T, s.A, s.D);
+    s.nodes += (__float_as_uint(An) ^ __float_as_uint(s.A)) >> 31;
+    s.A = An;
+}
+
+// renormalise (exact powers of two) and sample the peak at point i
+__device__ __forceinline__ void renorm32s(Side32& s, int i) {
+    const float mm = fmaxf(fabsf(s.A), fabsf(s.D));
+    const int e = ((__float_as_int(mm) >> 23) & 0xff) - 126;
+    if (mm > 0.0f && e > -60 && e < 60) {
+        const float sc = __int_as_float((127 - e) << 23);
+        s.A *= sc;
+        s.D *= sc;
+        s.S *= sc * sc;
+        s.ecum += e;
+    }
+    const int L = s.ecum + ((__float_as_int(fabsf(s.A)) >> 23) & 0xff);
+    if (s.A != 0.0f && L > s.Lpk) {
+        s.Lpk = L;
+        s.ipk = i;
+    }
+}
+
+// steps base.. of one side alone (points from + dir * step, nsteps in all),
+// in 8-step chunks renormalised at their ends; grid values do not depend on
+// the state, so two chunks are kept in flight (register double buffer)
+__device__ __forceinline__ void side32_rest(Side32& s, const float2* __restrict__ Wf, float aEh, float aEl, int from,
+                                            int dir, int base, int nsteps) {
+    auto load8 = [&](float2* w8, int b0) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) w8[u] = __ldg(Wf + from + dir * min(b0 + u, nsteps - 1));
+    };
+    auto run8 = [&](const float2* w8, int b0) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+            if (b0 + u < nsteps) step32s(s, aEh, aEl, w8[u]);
+        renorm32s(s, from + dir * min(b0 + 7, nsteps - 1));
+    };
+    float2 wa[8], wb[8];
+    if (base < nsteps) load8(wa, base);
+    for (int b0 = base; b0 < nsteps; b0 += 16) {
+        if (b0 + 8 < nsteps) load8(wb, b0 + 8);
+        run8(wa, b0);
+        if (b0 + 8 >= nsteps) break;
+        if (b0 + 16 < nsteps) load8(wa, b0 + 16);
+        run8(wb, b0 + 8);
+    }
+}
+
 __device__ __forceinline__ Pass32 cooley32(const PotMeta& m, const float2* __restrict__ Wf, const double* __restrict__ W64,
                                            double E, int k, int j0, int j1) {
     const double aE = __dmul_rn(m.a, E);
     const float aEh = __double2float_rn(aE);
     const float aEl = __double2float_rn(aE - (double)aEh);
-    float Ao = 1.f, Do = 1.f, So = 0.f, Ai = 1.f, Di = 1.f, Si = 0.f;
-    int Lk[2] = {0, 0}, Lpk[2] = {-(1 << 30), -(1 << 30)}, ipk[2] = {j0, j1};
-    int nodes = 0;
-    for (int side = 0; side < 2; ++side) {
-        float A = 1.0f, D = 1.0f, S = 0.0f;
-        const int from = side == 0 ? j0 : j1;
-        const int to = k;
-        const int dir = side == 0 ? 1 : -1;
-        int ecum = 0;
-        const int nsteps = (to - from) * dir;
-        // grid values do not depend on the state: two 8-point chunks in flight
-        // (register double buffer) hide the load latency behind the recurrence
-        auto load8 = [&](float2* w8, int base) {
+    // outward from j0 (u_{j0} = 1, u_{j0-1} = 0) and inward from j1, both to k
+    Side32 o{1.0f, 1.0f, 0.0f, 0, 0, -(1 << 30), j0};
+    Side32 in{1.0f, 1.0f, 0.0f, 0, 0, -(1 << 30), j1};
+    const int no = k - j0, ni = j1 - k;
+    // the two sides are independent recurrences: their common full chunks run
+    // interleaved (two dependency chains per lane), the rest of the longer
+    // side alone; the arithmetic of each side is unchanged
+    const int nb = min(no, ni) & ~7;
+    int base = 0;
+    for (; base < nb; base += 8) {
+        float2 wo[8], wi[8];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) w8[u] = __ldg(Wf + from + dir * min(base + u, nsteps - 1));
-        };
-        auto run8 = [&](const float2* w8, int base) {
+        for (int u = 0; u < 8; ++u) {
+            wo[u] = __ldg(Wf + j0 + base + u);
+            wi[u] = __ldg(Wf + j1 - base - u);
+        }
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                if (base + u < nsteps) {
-                    const float2 w = w8[u];
-                    const float T = (aEh - w.x) + (aEl - w.y);
-                    const float f = 1.0f + T;
-                    S = fmaf(f * f, S, A * A);
-                    const float X = fmaf(-12.0f, A, D);
-                    D = fmaf(T, X, D);
-                    const float An = A + fmaf(T, A, D);
-                    nodes += (__float_as_uint(An) ^ __float_as_uint(A)) >> 31;
-                    A = An;
-                }
-            }
-            const int i = from + dir * min(base + 7, nsteps - 1);
-            const float mm = fmaxf(fabsf(A), fabsf(D));
-            const int e = ((__float_as_int(mm) >> 23) & 0xff) - 126;
-            if (mm > 0.0f && e > -60 && e < 60) {
-                const float sc = __int_as_float((127 - e) << 23);
-                A *= sc;
-                D *= sc;
-                S *= sc * sc;
-                ecum += e;
-            }
-            const int L = ecum + ((__float_as_int(fabsf(A)) >> 23) & 0xff);
-            if (A != 0.0f && L > Lpk[side]) {
-                Lpk[side] = L;
-                ipk[side] = i;
-            }
-        };
-        float2 wa[8], wb[8];
-        if (nsteps > 0) load8(wa, 0);
-        for (int base = 0; base < nsteps; base += 16) {
-            if (base + 8 < nsteps) load8(wb, base + 8);
-            run8(wa, base);
-            if (base + 8 >= nsteps) break;
-            if (base + 16 < nsteps) load8(wa, base + 16);
-            run8(wb, base + 8);
+        for (int u = 0; u < 8; ++u) {
+            step32s(o, aEh, aEl, wo[u]);
+            step32s(in, aEh, aEl, wi[u]);
         }
-        Lk[side] = ecum + (A != 0.0f ? ((__float_as_int(fabsf(A)) >> 23) & 0xff) : -1000);
-        if (side == 0) {
-            Ao = A;
-            Do = D;
-            So = S;
-        } else {
-            Ai = A;
-            Di = D;
-            Si = S;
-        }
+        renorm32s(o, j0 + base + 7);
+        renorm32s(in, j1 - base - 7);
     }
+    side32_rest(o, Wf, aEh, aEl, j0, +1, base, no);
+    side32_rest(in, Wf, aEh, aEl, j1, -1, base, ni);
+    const int nodes = o.nodes + in.nodes;
+    const float Ao = o.A, Do = o.D, So = o.S, Ai = in.A, Di = in.D, Si = in.S;
+    const int Lk[2] = {o.ecum + (o.A != 0.0f ? ((__float_as_int(fabsf(o.A)) >> 23) & 0xff) : -1000),
+                       in.ecum + (in.A != 0.0f ? ((__float_as_int(fabsf(in.A)) >> 23) & 0xff) : -1000)};
+    const int Lpk[2] = {o.Lpk, in.Lpk}, ipk[2] = {o.ipk, in.ipk};
     const double Tk = aE - W64[k];
     const double fk = 1.0 + Tk;
     const double uA = Ao, vC = Ai;
@@ -286,7 +313,7 @@ __device__ __forceinline__ Pass32 cooley32(const PotMeta& m, const float2* __res
 // on the far side of the predicted root, or the level continues by bisection.
 constexpr double kTol32 = 2e-9;
 
-__global__ void __launch_bounds__(kLevelThreads) refine32_kernel(DevBatch b) {
+__global__ void __launch_bounds__(kLevelThreads, 4) refine32_kernel(DevBatch b) {
     for (int2 unit; next_unit(b, kQRefine32, unit);) {
         if ((int)(threadIdx.x & 31) >= unit.y) continue;
         const int slot = unit.x + (threadIdx.x & 31);

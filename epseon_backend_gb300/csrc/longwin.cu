@@ -275,6 +275,7 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
     }
     dfl q = Px.v;
     int eQ = Px.e;
+    PsiTag tag = psi_tag(MODE == 3 ? eA + eQ : 0);  // the stored pairs' scale and tag
     int nodes = 0;
     double S = 0.0;
     SqSum ss;
@@ -314,11 +315,7 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
                 const float p = __fmul_rn(psi.h, psi.h);
                 const float e = __fmaf_rn(psi.h, psi.h, -p);
                 ss.add({p, __fmaf_rn(2.0f * psi.h, psi.l, e)});
-                if (MODE == 3) {
-                    // psi-hat in the absolute scale 2^(eA + eQ) (as side_df)
-                    const int X = max(-900, min(900, eA + eQ));
-                    out[i] = f2d_pow2(psi.h, X) + f2d_pow2(psi.l, X);
-                }
+                if (MODE == 3 && out) store_psi_pair(out, i, psi, tag);  // absolute scale (as side_df)
             } else {
                 const dfl v = df_mul(psi, F);
                 out[i] = f2d(v.h) + f2d(v.l);
@@ -346,6 +343,7 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
                 eQ += eq;
                 if (kSums) {
                     ss.rescale(-2 * (e + eq));
+                    if (MODE == 3) tag = psi_tag(eA + eQ);
                     const float mag = fabsf(__fmul_rn(A.h, q.h));
                     if (mag > 0.0f) {
                         const int Lm = fexp(mag) + eA + eQ;
@@ -453,7 +451,7 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
 }
 
 // One pass at E with match point k (the CTA twin of pass_df<MODE>, MODE 0/1).
-// MODE 3 also stores the unnormalised psi-hat of the window in row.
+// MODE 3 also stores the unnormalised psi-hat of the window in row (if not null).
 template <int MODE>
 __device__ PassDF long_pass(const PotMeta& m, const LevelWork& w, const float2* __restrict__ Wf,
                             const double* __restrict__ W64, double E, int k, double sum_fallback, LongShared& sh,
@@ -966,9 +964,7 @@ __global__ void __launch_bounds__(kLongThreads) norm_long_kernel(DevBatch b) {
         const float2* Wf = b.Wf2 + m.offf;
         const double* W = b.W64 + m.off;
         double* row = psi_row(b, m, w);
-        auto pass = [&](int kk) {
-            return row ? long_pass<3>(m, w, Wf, W, w.E, kk, 1.0, sh, row) : long_pass<1>(m, w, Wf, W, w.E, kk, 1.0, sh);
-        };
+        auto pass = [&](int kk) { return long_pass<3>(m, w, Wf, W, w.E, kk, 1.0, sh, row); };
         int k = w.k;
         PassDF r = pass(k);
         if (r.peak_log2 >= 2) {
@@ -1040,9 +1036,7 @@ __global__ void __launch_bounds__(kLongThreads) twist_long_kernel(DevBatch b) {
         long_side<5>(Wf, aE, w.j1, w.j0, -1, nullptr, 0.0, 0, sh, &tw);
         const int k = clamp_k(w, tw.k == 0x7fffffff ? w.k : tw.k);
         double* row = psi_row(b, m, w);
-        auto pass = [&](double e) {
-            return row ? long_pass<3>(m, w, Wf, W, e, k, 1.0, sh, row) : long_pass<1>(m, w, Wf, W, e, k, 1.0, sh);
-        };
+        auto pass = [&](double e) { return long_pass<3>(m, w, Wf, W, e, k, 1.0, sh, row); };
         double E1 = w.E;
         PassDF r = pass(E1);
         for (int it = 0; it < 8; ++it) {
@@ -1067,6 +1061,8 @@ __global__ void __launch_bounds__(kLongThreads) twist_long_kernel(DevBatch b) {
     }
 }
 
+// psi of the long levels in FP64 from the final constants (window points and
+// psi_k; the rest of each row is zero): the adjoint's recompute path.
 __global__ void __launch_bounds__(kLongThreads) write_long_kernel(DevBatch b) {
     __shared__ LongShared sh;
     if (!b.psi || b.hdr->error) return;

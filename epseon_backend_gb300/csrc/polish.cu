@@ -38,120 +38,167 @@ constexpr int kThreads = 128;
 
 // MODE 0: state only (Newton)   MODE 1: + sums, psi-hat, peak   MODE 2: + write
 // MODE 3: MODE 1 + psi-hat written unnormalised (absolute scale, FP64)
+//
+// One side of a pass: the double-float state marched one point at a time
+// (step) and renormalised every 8 points (renorm).
 template <int MODE>
 struct SideDF {
     dfl A, D, q;      // state ~ s (u_i, u_i - u_{i-1}); q = 1/s (MODE >= 1)
     int eA, eQ;       // exponents removed from (A, D) and from q
     int nodes;
-    double S;         // MODE 1/3: sum of psi-hat^2 in the current stored scale (FP64)
+    SqSum ss;         // MODE 1/3: sum of psi-hat^2 in the current scale
+    double S;         // MODE 1/3: that sum at the end of the side (FP64)
+    PsiTag tag;       // MODE 3: scale and tag of the stored pair (X = eA + eQ)
     int peak_L, peak_i;
-};
+    dfl F;            // MODE 2: psi scale constant in the current scale
+    double L;         // MODE 2: the side's norm constant
+    int Xk;           //   and its exponent
 
-template <int MODE>
-__device__ __forceinline__ void side_df(const float2* __restrict__ Wf, dfl aE, int from, int to, int dir,
-                                        SideDF<MODE>& st, double* __restrict__ out, double L, int Xk) {
-    st.A = {1.0f, 0.0f};
-    st.D = {1.0f, 0.0f};  // u_from = 1, u_{from-dir} = 0
-    st.q = {1.0f, 0.0f};
-    st.eA = st.eQ = 0;
-    st.nodes = 0;
-    st.S = 0.0;
-    st.peak_L = -(1 << 30);
-    st.peak_i = from;
-    SqSum ss;  // MODE 1/3: sum of psi-hat^2 in the current scale
-    ss.init();
-    dfl F = {0.0f, 0.0f};
-    if (MODE == 2) F = df_from_double(L * pow2(min(1000, max(-1000, -Xk))));
-    const int nsteps = (to - from) * dir;
-    auto load8 = [&](float2* w8, int base) {
-#pragma unroll
-        for (int u = 0; u < 8; ++u) w8[u] = __ldg(Wf + from + dir * min(base + u, nsteps - 1));
-    };
-    auto run8 = [&](const float2* w8, int base) {
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            if (base + u >= nsteps) break;
-            const int i = from + dir * (base + u);
-            const float2 w = w8[u];
-            dfl T = two_sum(aE.h, -w.x);
-            T = fast_two_sum(T.h, __fadd_rn(T.l, __fsub_rn(aE.l, w.y)));
-            if (MODE >= 1) {
-                const dfl f = df_add({1.0f, 0.0f}, T);
-                const dfl qn = df_mul(st.q, df_recip(f));
-                const dfl psi = df_mul(st.A, qn);  // psi-hat_i = A_i / s_{i+1}
-                if (MODE == 1 || MODE == 3) {
-                    const float p = __fmul_rn(psi.h, psi.h);
-                    const float e = __fmaf_rn(psi.h, psi.h, -p);
-                    ss.add({p, __fmaf_rn(2.0f * psi.h, psi.l, e)});
-                    if (MODE == 3) {
-                        // psi-hat in the absolute scale 2^(eA + eQ): exact bit
-                        // constructions and one FP64 add
-                        const int X = max(-900, min(900, st.eA + st.eQ));
-                        out[i] = f2d_pow2(psi.h, X) + f2d_pow2(psi.l, X);
-                    }
-                } else {
-                    const dfl v = df_mul(psi, F);
-                    out[i] = f2d(v.h) + f2d(v.l);
-                }
-                st.q = qn;
+    __device__ __forceinline__ void init(int from, double L_, int Xk_) {
+        A = {1.0f, 0.0f};
+        D = {1.0f, 0.0f};  // u_from = 1, u_{from-dir} = 0
+        q = {1.0f, 0.0f};
+        eA = eQ = 0;
+        nodes = 0;
+        ss.init();
+        S = 0.0;
+        peak_L = -(1 << 30);
+        peak_i = from;
+        tag = psi_tag(0);
+        L = L_;
+        Xk = Xk_;
+        F = {0.0f, 0.0f};
+        if (MODE == 2) F = df_from_double(L * pow2(min(1000, max(-1000, -Xk))));
+    }
+
+    // the step at point i (grid value w)
+    __device__ __forceinline__ void step(dfl aE, float2 w, double* __restrict__ out, int i) {
+        dfl T = two_sum(aE.h, -w.x);
+        T = fast_two_sum(T.h, __fadd_rn(T.l, __fsub_rn(aE.l, w.y)));
+        if (MODE >= 1) {
+            const dfl f = df_add({1.0f, 0.0f}, T);
+            const dfl qn = df_mul(q, df_recip(f));
+            const dfl psi = df_mul(A, qn);  // psi-hat_i = A_i / s_{i+1}
+            if (MODE == 1 || MODE == 3) {
+                const float p = __fmul_rn(psi.h, psi.h);
+                const float e = __fmaf_rn(psi.h, psi.h, -p);
+                ss.add({p, __fmaf_rn(2.0f * psi.h, psi.l, e)});
+                if (MODE == 3) store_psi_pair(out, i, psi, tag);  // absolute scale
+            } else {
+                const dfl v = df_mul(psi, F);
+                out[i] = f2d(v.h) + f2d(v.l);
             }
-            const dfl X = df_add(st.D, df_mulf(st.A, -12.0f));
-            st.D = df_add(st.D, df_mul(T, X));
-            const dfl An = df_add(st.A, df_add(df_mul(T, st.A), st.D));
-            st.nodes += (__float_as_uint(An.h) ^ __float_as_uint(st.A.h)) >> 31;
-            st.A = An;
+            q = qn;
         }
-        // renormalise every 8 steps (exact powers of two)
-        const int i = from + dir * min(base + 7, nsteps - 1);
-        const float mm = fmaxf(fabsf(st.A.h), fabsf(st.D.h));
+        const dfl X = df_add(D, df_mulf(A, -12.0f));
+        D = df_add(D, df_mul(T, X));
+        const dfl An = df_add(A, df_add(df_mul(T, A), D));
+        nodes += (__float_as_uint(An.h) ^ __float_as_uint(A.h)) >> 31;
+        A = An;
+    }
+
+    // renormalise (exact powers of two) after the step at point i
+    __device__ __forceinline__ void renorm(int i) {
+        const float mm = fmaxf(fabsf(A.h), fabsf(D.h));
         int e = 0, eq = 0;
         if (mm > 0.0f && mm < INFINITY) {
             e = max(-120, min(120, fexp(mm)));
             const float sc = fpow2(-e);
-            st.A = df_scale(st.A, sc);
-            st.D = df_scale(st.D, sc);
-            st.eA += e;
+            A = df_scale(A, sc);
+            D = df_scale(D, sc);
+            eA += e;
         }
         if (MODE >= 1) {
-            eq = max(-120, min(120, fexp(st.q.h)));
-            st.q = df_scale(st.q, fpow2(-eq));
-            st.eQ += eq;
+            eq = max(-120, min(120, fexp(q.h)));
+            q = df_scale(q, fpow2(-eq));
+            eQ += eq;
             if (MODE == 1 || MODE == 3) {
                 ss.rescale(-2 * (e + eq));
-                const float mag = fabsf(__fmul_rn(st.A.h, st.q.h));
+                if (MODE == 3) tag = psi_tag(eA + eQ);
+                const float mag = fabsf(__fmul_rn(A.h, q.h));
                 if (mag > 0.0f) {
-                    const int Lm = fexp(mag) + st.eA + st.eQ;
-                    if (Lm > st.peak_L) {
-                        st.peak_L = Lm;
-                        st.peak_i = i;
+                    const int Lm = fexp(mag) + eA + eQ;
+                    if (Lm > peak_L) {
+                        peak_L = Lm;
+                        peak_i = i;
                     }
                 }
             } else if (e + eq != 0) {
-                F = df_from_double(L * pow2(min(1000, max(-1000, st.eA + st.eQ - Xk))));
+                F = df_from_double(L * pow2(min(1000, max(-1000, eA + eQ - Xk))));
             }
         }
-        };
-    // one 8-point chunk in flight: the double-float body is long enough to hide
-    // the load behind the other resident warps (a second buffer costs occupancy)
-    for (int base = 0; base < nsteps; base += 8) {
-        float2 w8[8];
-        load8(w8, base);
-        run8(w8, base);
     }
-    if (MODE == 1 || MODE == 3) st.S = ss.value();
+};
+
+// steps base..nsteps-1 of a side alone (point from + dir * step), 8-step
+// chunks renormalised at their ends; one chunk in flight (the double-float
+// body is long enough to hide the load behind the other resident warps)
+template <int MODE>
+__device__ __forceinline__ void side_df_rest(SideDF<MODE>& st, const float2* __restrict__ Wf, dfl aE, int from,
+                                             int dir, int base, int nsteps, double* __restrict__ out) {
+    for (int b0 = base; b0 < nsteps; b0 += 8) {
+        float2 w8[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) w8[u] = __ldg(Wf + from + dir * min(b0 + u, nsteps - 1));
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            if (b0 + u >= nsteps) break;
+            st.step(aE, w8[u], out, from + dir * (b0 + u));
+        }
+        st.renorm(from + dir * min(b0 + 7, nsteps - 1));
+    }
+}
+
+// one side on its own (the write pass)
+template <int MODE>
+__device__ __forceinline__ void side_df(const float2* __restrict__ Wf, dfl aE, int from, int to, int dir,
+                                        SideDF<MODE>& st, double* __restrict__ out, double L, int Xk) {
+    st.init(from, L, Xk);
+    side_df_rest(st, Wf, aE, from, dir, 0, (to - from) * dir, out);
+    if (MODE == 1 || MODE == 3) st.S = st.ss.value();
 }
 
 // one pass at E with match point k over the level's window [w.j0, w.j1];
 // MODE 0: gamma/count only, MODE 1: + sums, MODE 3: + unnormalised psi-hat
-// into row (the level's psi row)
-template <int MODE>
+// into row (the level's psi row).  PAIRED: the outward and inward sides are
+// independent recurrences, so their common full chunks can run interleaved
+// (two dependency chains per lane) and the rest of the longer side alone; the
+// arithmetic of each side is unchanged.  (Measured on GB300: slower for both
+// the state-only Newton pass and the norm pass, whose doubled loop bodies
+// cost more than the second chain gains; the FP32 lane pass, with a far
+// shorter step, does gain from it.)
+template <int MODE, bool PAIRED>
 __device__ PassDF pass_df(const PotMeta& m, const LevelWork& w, const float2* __restrict__ Wf,
                           const double* __restrict__ W64, double E, int k, double sum_fallback,
                           double* __restrict__ row = nullptr) {
     const dfl aE = energy_df(m, E);
     SideDF<MODE> o, in;
-    side_df<MODE>(Wf, aE, w.j0, k, +1, o, row, 0.0, 0);
-    side_df<MODE>(Wf, aE, w.j1, k, -1, in, row, 0.0, 0);
+    o.init(w.j0, 0.0, 0);
+    in.init(w.j1, 0.0, 0);
+    const int no = k - w.j0, ni = w.j1 - k;
+    const int nb = PAIRED ? (min(no, ni) & ~7) : 0;
+    int base = 0;
+    for (; base < nb; base += 8) {
+        float2 wo[8], wi[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            wo[u] = __ldg(Wf + w.j0 + base + u);
+            wi[u] = __ldg(Wf + w.j1 - base - u);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            o.step(aE, wo[u], row, w.j0 + base + u);
+            in.step(aE, wi[u], row, w.j1 - base - u);
+        }
+        o.renorm(w.j0 + base + 7);
+        in.renorm(w.j1 - base - 7);
+    }
+    side_df_rest(o, Wf, aE, w.j0, +1, base, no, row);
+    side_df_rest(in, Wf, aE, w.j1, -1, base, ni, row);
+    if (MODE == 1 || MODE == 3) {
+        o.S = o.ss.value();
+        in.S = in.ss.value();
+    }
     const double Tk = __dsub_rn(__dmul_rn(m.a, E), __ldg(W64 + k));
     const double fk = 1.0 + Tk;
     const double Ao = df_to_double(o.A), Do = df_to_double(o.D);
@@ -199,7 +246,7 @@ __global__ void __launch_bounds__(kThreads, 4) newton_df_kernel(DevBatch b) {
         bool ok = false;
         int n_pass = 0;
         for (int it = 0; it < 4 && !ok; ++it) {
-            const PassDF r = pass_df<0>(m, w, Wf, W, E, w.k, w.norm_k_in);
+            const PassDF r = pass_df<0, false>(m, w, Wf, W, E, w.k, w.norm_k_in);
             ++n_pass;
             if (r.count > w.v) hi = fmin(hi, E);
             else lo = fmax(lo, E);
@@ -245,7 +292,7 @@ __global__ void __launch_bounds__(kThreads, 4) norm_df_kernel(DevBatch b) {
         int n_pass = 0;
         auto pass = [&](int kk) {
             ++n_pass;
-            return row ? pass_df<3>(m, w, Wf, W, w.E, kk, 1.0, row) : pass_df<1>(m, w, Wf, W, w.E, kk, 1.0);
+            return row ? pass_df<3, false>(m, w, Wf, W, w.E, kk, 1.0, row) : pass_df<1, false>(m, w, Wf, W, w.E, kk, 1.0);
         };
         // match point candidates: the FP32 one, the peak of |psi| seen by this
         // pass, the outer turning point and its peak; the first whose
@@ -336,7 +383,7 @@ __global__ void __launch_bounds__(256) zero_psi_kernel(DevBatch b) {
 
 // The write-back of the fused norm/write: each row holds the unnormalised
 // psi-hat of the level's final norm pass (norm_df, norm_long or twist_long)
-// on [j0, k) and (k, j1]; scale it by the
+// on [j0, k) and (k, j1] as scaled float pairs; scale it by the
 // side constants (norm_k 2^-ex) and set psi_k = ck.  The rest of the row was
 // zeroed by zero_psi.  One warp per level, coalesced: HBM-bound (8 B read +
 // 8 B written per window point).
@@ -351,10 +398,27 @@ __global__ void __launch_bounds__(256) scale_psi_kernel(DevBatch b) {
         const PotMeta m = b.meta[w.p];
         double* row = b.psi + m.psi_off + (int64_t)(w.v - b.min_level) * m.N;
         if (no_result(w)) continue;
-        const double c_out = w.norm_k_out * pow2(max(-1000, min(1000, -w.ex_out)));
-        const double c_in = w.norm_k_in * pow2(max(-1000, min(1000, -w.ex_in)));
-        for (int i = w.j0 + lane; i <= w.j1; i += 32)
-            row[i] = i < w.k ? row[i] * c_out : (i > w.k ? row[i] * c_in : w.ck);
+        // the side constants norm_k 2^-ex as m 2^e, m in [0.5, 1) a
+        // double-float: per point the pair times m in double-float and the
+        // double assembled with integer operations, scaled by 2^(64 r + e)
+        // in its exponent bits (no FP64 instruction per point)
+        int e_out, e_in;
+        const dfl M_out = df_from_double(frexp(w.norm_k_out, &e_out));
+        const dfl M_in = df_from_double(frexp(w.norm_k_in, &e_in));
+        e_out -= w.ex_out;
+        e_in -= w.ex_in;
+        const float2* pair = reinterpret_cast<const float2*>(row);
+        for (int i = w.j0 + lane; i <= w.j1; i += 32) {
+            if (i == w.k) {
+                row[i] = w.ck;
+                continue;
+            }
+            int r;
+            const dfl v = load_psi_pair(pair[i], r);
+            const bool outward = i < w.k;
+            const dfl p = df_mul(v, outward ? M_out : M_in);
+            row[i] = df_pair_to_double_scaled(p.h, p.l, 64 * r + (outward ? e_out : e_in));
+        }
     }
 }
 

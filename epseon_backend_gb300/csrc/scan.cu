@@ -399,8 +399,11 @@ void set_attr_t() {
 }  // namespace
 
 void scan32_set_attributes() {
+    set_attr_t<128, 1024, 2>();
     set_attr_t<128, 1024, 4>();
+    set_attr_t<128, 2048, 2>();
     set_attr_t<128, 2048, 3>();
+    set_attr_t<256, 1024, 2>();
     set_attr_t<256, 1024, 4>();
     set_attr_t<256, 2048, 3>();
     set_attr_t<256, 4096, 2>();
@@ -421,8 +424,11 @@ void launch_scan32(const DevBatch& b, const ScanShape& sh, int sm_count, cudaStr
         launch_scan32_t<TH, TI, ST>(b, sh.ctas_per_sm, sm_count, s);               \
         return;                                                                    \
     }
+    EPSCU_SCAN32_CASE(128, 1024, 2)
     EPSCU_SCAN32_CASE(128, 1024, 4)
+    EPSCU_SCAN32_CASE(128, 2048, 2)
     EPSCU_SCAN32_CASE(128, 2048, 3)
+    EPSCU_SCAN32_CASE(256, 1024, 2)
     EPSCU_SCAN32_CASE(256, 1024, 4)
     EPSCU_SCAN32_CASE(256, 2048, 3)
     EPSCU_SCAN32_CASE(256, 4096, 2)
