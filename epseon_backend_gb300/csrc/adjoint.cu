@@ -23,11 +23,17 @@ namespace {
 // accumulate = add into dL_dV instead of storing.  One CTA per (potential,
 // 256 points); the CTA first narrows the level loop to the levels whose
 // window meets its points (windows grow with the level, so near the ends of
-// a grid only the highest levels remain).
+// a grid only the highest levels remain), stages their windows and dL/dE in
+// shared memory, and reads four rows per step (four loads in flight per
+// thread: the kernel is bound by HBM latency otherwise).
+constexpr int kAdjTile = 256;  // levels staged per round
+
 __global__ void __launch_bounds__(256) adjoint_kernel(DevBatch b, const double* __restrict__ gE, double* __restrict__ gV,
                                                       const int64_t* __restrict__ offsets, const double* __restrict__ psi,
                                                       int accumulate) {
     __shared__ int s_lo, s_hi;
+    __shared__ int2 s_win[kAdjTile];
+    __shared__ double s_g[kAdjTile];
     const int p = blockIdx.y;
     const PotMeta m = b.meta[p];
     const int i_a = blockIdx.x * blockDim.x;
@@ -46,16 +52,39 @@ __global__ void __launch_bounds__(256) adjoint_kernel(DevBatch b, const double* 
         }
     }
     __syncthreads();
+    const int lo = s_lo, hi = s_hi;
     const int i = i_a + threadIdx.x;
-    if (i > i_b) return;
     const double* rows = psi + m.psi_off + i;
     const double* g = gE + (int64_t)p * b.level_capacity;
     double acc = 0.0;
-    for (int s = s_lo; s <= s_hi; ++s) {
-        if (i < lw[s].j0 || i > lw[s].j1) continue;
-        const double v = __ldg(rows + (int64_t)s * m.N);
-        acc = fma(g[s] * v, v, acc);
+    for (int t0 = lo; t0 <= hi; t0 += kAdjTile) {
+        const int nt = min(kAdjTile, hi - t0 + 1);
+        __syncthreads();  // the previous round's stage is consumed
+        for (int q = threadIdx.x; q < nt; q += blockDim.x) {
+            s_win[q] = make_int2(lw[t0 + q].j0, lw[t0 + q].j1);
+            s_g[q] = g[t0 + q];
+        }
+        __syncthreads();
+        if (i > i_b) continue;
+        // (a level's term is added only inside its window, as if the loop
+        // skipped the others: a non-finite dL/dE stays out of their sums)
+        auto inside = [&](int q) {
+            const int2 wq = s_win[q];
+            return i >= wq.x && i <= wq.y;
+        };
+        auto load = [&](int q) { return inside(q) ? __ldg(rows + (int64_t)(t0 + q) * m.N) : 0.0; };
+        auto add = [&](int q, double v) { acc = inside(q) ? fma(s_g[q] * v, v, acc) : acc; };
+        int q = 0;
+        for (; q + 3 < nt; q += 4) {
+            const double v0 = load(q), v1 = load(q + 1), v2 = load(q + 2), v3 = load(q + 3);
+            add(q, v0);
+            add(q + 1, v1);
+            add(q + 2, v2);
+            add(q + 3, v3);
+        }
+        for (; q < nt; ++q) add(q, load(q));
     }
+    if (i > i_b) return;
     acc *= m.h;
     if (accumulate) gV[offsets[p] + i] += acc;
     else gV[offsets[p] + i] = acc;

@@ -408,17 +408,24 @@ __global__ void __launch_bounds__(256) scale_psi_kernel(DevBatch b) {
         e_out -= w.ex_out;
         e_in -= w.ex_in;
         const float2* pair = reinterpret_cast<const float2*>(row);
-        for (int i = w.j0 + lane; i <= w.j1; i += 32) {
-            if (i == w.k) {
-                row[i] = w.ck;
-                continue;
-            }
+        auto convert = [&](int i, float2 raw) {
             int r;
-            const dfl v = load_psi_pair(pair[i], r);
+            const dfl v = load_psi_pair(raw, r);
             const bool outward = i < w.k;
             const dfl p = df_mul(v, outward ? M_out : M_in);
-            row[i] = df_pair_to_double_scaled(p.h, p.l, 64 * r + (outward ? e_out : e_in));
+            return i == w.k ? w.ck : df_pair_to_double_scaled(p.h, p.l, 64 * r + (outward ? e_out : e_in));
+        };
+        // four points per lane per step: four loads in flight (the kernel is
+        // bound by HBM latency with one)
+        int i = w.j0 + lane;
+        for (; i + 96 <= w.j1; i += 128) {
+            const float2 r0 = pair[i], r1 = pair[i + 32], r2 = pair[i + 64], r3 = pair[i + 96];
+            row[i] = convert(i, r0);
+            row[i + 32] = convert(i + 32, r1);
+            row[i + 64] = convert(i + 64, r2);
+            row[i + 96] = convert(i + 96, r3);
         }
+        for (; i <= w.j1; i += 32) row[i] = convert(i, pair[i]);
     }
 }
 
