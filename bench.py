@@ -365,12 +365,25 @@ def main():
     batch_host = capi.Concatenated(V_pinned.numpy(), offsets, N)
     e2e_steps = max(2, args.steps // 2)
     maskh = (np.arange(cap)[None, :] < ref.n_out[:, None])
+    w2m = 2.0 * w_np * maskh
+
+    # page-locked host buffers, allocated once: the solve's results and the
+    # loss gradient dL/dE (the host side of a training loop would keep these)
+    def pinned(shape, dtype):
+        return torch.empty(shape, dtype=dtype).pin_memory().numpy()
+
+    nb = len(b)
+    res_buf = capi.Solution(pinned((nb,), torch.int32), pinned((nb,), torch.int32), pinned((nb, cap), torch.float64),
+                            pinned((nb, cap), torch.int32), pinned((nb, cap), torch.int32),
+                            pinned((nb, cap), torch.float64), None, pinned((nb,), torch.int64), N)
+    gE_pinned = pinned((nb, cap), torch.float64)
 
     def e2e_step():
         sol = ctx.solve(batch_host, b.r_min, b.r_max, b.mu, b.e_cap, b.n_trial, method=capi.METHOD_FAST_FP32C,
-                        level_capacity=cap, keep_psi=True, long_window=args.long_window)
-        gEh = 2.0 * w_np * (np.nan_to_num(sol.energy) - target_np) * maskh
-        return sol, gEh, ctx.adjoint(gEh, Vcat.size, recompute=False, out=gV_pinned.numpy())
+                        level_capacity=cap, keep_psi=True, long_window=args.long_window, out=res_buf)
+        np.subtract(np.nan_to_num(sol.energy), target_np, out=gE_pinned)
+        np.multiply(gE_pinned, w2m, out=gE_pinned)
+        return sol, gE_pinned, ctx.adjoint(gE_pinned, Vcat.size, recompute=False, out=gV_pinned.numpy())
 
     e2e_step()
     torch.cuda.synchronize()

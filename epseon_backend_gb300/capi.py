@@ -310,8 +310,13 @@ class Context:
         tune: bool = False,
         long_window: int = 0,
         keep_psi: bool = False,
+        out: Solution | None = None,
     ) -> Solution:
-        """Solve a batch of host potentials (host buffers through the C ABI)."""
+        """Solve a batch of host potentials (host buffers through the C ABI).
+
+        out: a Solution of this batch's shape whose result arrays are written
+        in place (for instance page-locked buffers reused across solves, so
+        the device-to-host copies run at full speed); its psi is not used."""
         V, offsets, N = concat(Vs)
         n = int(N.size)
 
@@ -323,13 +328,26 @@ class Context:
         if level_capacity is None:
             level_capacity = (max_level - min_level + 1) if max_level >= 0 else 512
         cap = int(level_capacity)
-        n_total = np.zeros(n, np.int32)
-        n_out = np.zeros(n, np.int32)
-        energy = np.zeros((n, cap))
-        nodes = np.zeros((n, cap), np.int32)
-        status = np.zeros((n, cap), np.int32)
-        err = np.zeros((n, cap))
-        psi_off = np.zeros(n, np.int64)
+        if out is not None:
+            def own(a, shape, dtype):
+                if a.shape != shape or a.dtype != dtype or not a.flags.c_contiguous:
+                    raise ValueError(f"out array of shape {a.shape} {a.dtype}, expected {shape} {np.dtype(dtype)}")
+                return a
+            n_total = own(out.n_total, (n,), np.int32)
+            n_out = own(out.n_out, (n,), np.int32)
+            energy = own(out.energy, (n, cap), np.float64)
+            nodes = own(out.nodes, (n, cap), np.int32)
+            status = own(out.status, (n, cap), np.int32)
+            err = own(out.err_est, (n, cap), np.float64)
+            psi_off = own(out.psi_offsets, (n,), np.int64)
+        else:
+            n_total = np.zeros(n, np.int32)
+            n_out = np.zeros(n, np.int32)
+            energy = np.zeros((n, cap))
+            nodes = np.zeros((n, cap), np.int32)
+            status = np.zeros((n, cap), np.int32)
+            err = np.zeros((n, cap))
+            psi_off = np.zeros(n, np.int64)
         psi = None
         if want_psi:
             if psi_capacity is None:

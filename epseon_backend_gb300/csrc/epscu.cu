@@ -382,7 +382,10 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     // host buffers, no psi buffer, psi kept in device memory for the adjoint:
     // the psi size is read back after the level setup, then the rest runs
     const bool keep_psi = (opts.flags & EPSCU_KEEP_PSI) && !want_psi && !dev;
-    const bool stage_events = (opts.flags & EPSCU_STAGE_TIMING) != 0 || !dev;
+    // per-stage events (one stream, stages in sequence) only when asked for;
+    // otherwise the fast method's two branches run side by side, graph-replayed
+    // for device-resident inputs and launched directly for host buffers
+    const bool stage_events = (opts.flags & EPSCU_STAGE_TIMING) != 0;
     if (n <= 0) return fail(EPSCU_ERR_INVALID, "n_potentials must be positive");
     if (cap <= 0) return fail(EPSCU_ERR_INVALID, "level_capacity must be positive");
     if (method != EPSCU_METHOD_PLAIN_FP64 && method != EPSCU_METHOD_FAST_FP32C)
@@ -623,6 +626,7 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
         EPSCU_CU(cudaGraphLaunch(ctx->graph, s));
         EPSCU_CU(cudaEventRecord(ctx->ev[6], s));
     } else if (keep_psi) {
+        if (!stage_events) EPSCU_CU(cudaEventRecord(ctx->ev[0], s));
         EPSCU_CU(enqueue_inputs());
         enqueue_pipeline(ctx, b, method, true, shape, stage_events, s, 1);
         EPSCU_CU(cudaMemcpyAsync(hh, b.hdr, sizeof(Header), cudaMemcpyDeviceToHost, s));
@@ -633,10 +637,12 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
         b.psi_capacity = need;
         enqueue_pipeline(ctx, b, method, true, shape, stage_events, s, 2);
         launch_gather(b, o_nt, o_no, o_e, o_nd, o_st, o_err, method == EPSCU_METHOD_FAST_FP32C ? 1 : 0, s);
-        if (stage_events) EPSCU_CU(cudaEventRecord(ctx->ev[6], s));
+        EPSCU_CU(cudaEventRecord(ctx->ev[6], s));
         EPSCU_CU(cudaGetLastError());
     } else {
+        if (!stage_events) EPSCU_CU(cudaEventRecord(ctx->ev[0], s));
         EPSCU_CU(enqueue_all());
+        if (!stage_events) EPSCU_CU(cudaEventRecord(ctx->ev[6], s));
     }
 
     // ---- outputs back

@@ -809,7 +809,8 @@ __device__ __forceinline__ bool cancelled(const DevBatch& b) { return b.cancel &
 //   1. FP32 passes (long_pass32): safeguarded Cooley-Newton to |dE| <= 2e-9
 //      with the count bracket, the match point moved to the peak of |psi|;
 //   2. double-float state-only passes with the FP32 sum as the Newton
-//      denominator (as newton_df): one or two steps to 1e-12;
+//      denominator (as newton_df): usually one step, accepted from within
+//      1e-8 (the chunked FP32 sum is accurate to ~1e-6);
 //   3. if stage 2 does not settle (the FP32 counts are off near a trial
 //      energy, or the pass sees another node count): safeguarded
 //      Cooley-Newton in double-float with full sums from the scan bracket
@@ -884,7 +885,10 @@ __global__ void __launch_bounds__(kLongThreads) refine_long_kernel(DevBatch b, i
                     else lo2 = fmax(lo2, E);
                     const double En = E + r.dE;
                     if (!isfinite(En) || !(En >= lo2 && En <= hi2) || r.nodes != w.v) break;
-                    done = fabs(r.dE) <= (it == 0 ? 1e-10 : 1e-12 * fmax(1.0, fabs(E)));
+                    // the FP32 sum of the CTA pass is accurate to ~1e-6 (chunk
+                    // sums of a few hundred terms, added in FP64), so one step
+                    // from within 1e-8 leaves ~1e-14: the first pass settles
+                    done = fabs(r.dE) <= (it == 0 ? 1e-8 * fmax(1.0, fabs(E)) : 1e-12 * fmax(1.0, fabs(E)));
                     E = En;
                 }
                 if (done) {
