@@ -151,8 +151,18 @@ __device__ __forceinline__ int match_index(const PotMeta& m, const double* __res
     return lo;
 }
 
-// e-folds of decay at the ends of the fast method's windows
-constexpr float kWindowDecay = 46.0f;
+// bisection scan: the throughput scan on every kBisectCoarse-th trial
+// energy, then cells halved round by round
+constexpr int kBisectCoarse = 8;
+// batches of at least this many potentials take the bisection scan (smaller
+// ones have too few CTAs per round to cover its latency; measured on GB300)
+constexpr int kBisectMinPotentials = 512;
+
+// e-folds of decay at the ends of the fast method's windows: e^-36 = 2.3e-16,
+// psi at the cut is below FP64 resolution relative to its value at the
+// turning point (dense eigen-decompositions of the discrete problem keep
+// every level to 1e-12 and every eigenvector to 1e-10 in L2 down to 26)
+constexpr float kWindowDecay = 36.0f;
 // trial energies per entry of the scan's window table
 constexpr int kScanWinBlock = 128;
 

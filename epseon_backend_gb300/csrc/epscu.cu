@@ -305,6 +305,7 @@ void enqueue_pipeline(epscu_ctx* ctx, const DevBatch& b, int method, bool want_p
         if (method == EPSCU_METHOD_FAST_FP32C) launch_scan_window(b, ctx->sm_count, s);  // timed with prepare
         rec(1);
         if (method == EPSCU_METHOD_PLAIN_FP64) launch_scan64(b, s);
+        else if (b.bis_list) launch_bisect_scan(b, shape, ctx->sm_count, s);
         else launch_scan32(b, shape, ctx->sm_count, s);
         rec(2);
         launch_level_setup(b, s);
@@ -459,6 +460,8 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     b.order = (int32_t*)ctx->get("order", sizeof(int32_t) * n, &ce);
     b.scan_win = nullptr;
     b.long_list = nullptr;
+    b.bis_list = nullptr;
+    b.bis_n = nullptr;
     b.Mpre = nullptr;
     b.Bmin = nullptr;
     if (method == EPSCU_METHOD_FAST_FP32C) {
@@ -470,6 +473,12 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
         const size_t nb = (size_t)(batch->n_trial + kScanWinBlock - 1) / kScanWinBlock;
         b.scan_win = (int2*)ctx->get("scan_win", sizeof(int2) * (size_t)n * nb, &ce);
         if (!b.scan_win) return fail(EPSCU_ERR_NOMEM, "device arena (scan windows)");
+        if (n >= kBisectMinPotentials) {
+            // batches: the bisection scan (counts where they change only)
+            b.bis_list = (int32_t*)ctx->get("bis_list", sizeof(int32_t) * (size_t)n * batch->n_trial, &ce);
+            b.bis_n = (int32_t*)ctx->get("bis_n", sizeof(int32_t) * (size_t)n, &ce);
+            if (!b.bis_list || !b.bis_n) return fail(EPSCU_ERR_NOMEM, "device arena (bisection scan)");
+        }
     }
     int64_t* d_off = (int64_t*)ctx->get("offsets", sizeof(int64_t) * n, &ce);
     if (ce != cudaSuccess || !b.meta || !b.W64 || !b.Msuf || !b.counts || !b.levels || !b.fallback_list || !b.units ||
@@ -555,7 +564,7 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
         for (const ScanShape& c : cands) {
             EPSCU_CU(cudaMemsetAsync(&b.hdr->queue_scan, 0, sizeof(int32_t), s));
             EPSCU_CU(cudaEventRecord(ctx->ev[6], s));
-            launch_scan32(b, c, ctx->sm_count, s);
+            launch_scan32(b, c, ctx->sm_count, s, b.bis_list ? kBisectCoarse : 1);
             EPSCU_CU(cudaEventRecord(ctx->ev[7], s));
             EPSCU_CU(cudaEventSynchronize(ctx->ev[7]));
             EPSCU_CU(cudaGetLastError());
@@ -718,6 +727,7 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     // gather (+ zero_psi, scale_psi)
     const bool psi_kernels = want_psi || keep_psi;
     st.kernel_launches = method == EPSCU_METHOD_FAST_FP32C ? 16 + (psi_kernels ? 2 : 0) : 9 + (psi_kernels ? 1 : 0);
+    if (b.bis_list) st.kernel_launches += 6;  // three plan + count rounds after the coarse scan32
     if (method == EPSCU_METHOD_PLAIN_FP64) {
         st.refine_point_updates = 0;
         int64_t bis = 0;

@@ -34,6 +34,9 @@ struct DevBatch {
     int32_t* order;            // [n] potentials by decreasing cost
     int2* scan_win;            // [n * ceil(n_trial / kScanWinBlock)] scan windows, or nullptr (full grid)
     int32_t* long_list;        // [max_levels] slots with long windows (CTA-per-level passes), or nullptr
+    int32_t* bis_list;         // [n * n_trial] trial indices of the bisection scan's current round, or
+                               // nullptr (every trial energy scanned)
+    int32_t* bis_n;            // [n] entries of bis_list per potential
     double* psi;               // compact wavefunctions or nullptr
     int64_t psi_capacity;
     volatile int32_t* cancel;  // host-mapped cancel flag (device pointer) or nullptr
@@ -78,7 +81,8 @@ struct ScanShape {
     int stages;
     int ctas_per_sm;  // persistent grid = sm_count * ctas_per_sm
 };
-void launch_scan32(const DevBatch& b, const ScanShape& shape, int sm_count, cudaStream_t s);
+void launch_scan32(const DevBatch& b, const ScanShape& shape, int sm_count, cudaStream_t s, int stride = 1);
+void launch_bisect_scan(const DevBatch& b, const ScanShape& shape, int sm_count, cudaStream_t s);
 int scan32_max_tile();
 void scan32_set_attributes();
 

@@ -294,10 +294,35 @@ __global__ void bracket_kernel(DevBatch b) {
     for (int s = threadIdx.x; s < m.n_out; s += blockDim.x) {
         const int v = b.min_level + s;
         int lo = 0, hi = m.n_trial;
-        while (lo < hi) {
-            const int mid = lo + (hi - lo) / 2;
-            if (c[mid] > v) hi = mid;
-            else lo = mid + 1;
+        if (!b.bis_list) {
+            while (lo < hi) {
+                const int mid = lo + (hi - lo) / 2;
+                if (c[mid] > v) hi = mid;
+                else lo = mid + 1;
+            }
+        } else {
+            // bisection scan: counts exist at the coarse boundaries and at the
+            // midpoints of every cell that held a level; descend the same
+            // cells to the first trial index with a count above v
+            const int last = m.n_trial - 1;
+            const int ctop = c[last];
+            if (v >= ctop) {
+                lo = m.n_trial;
+            } else {
+                const int K = (m.n_trial + kBisectCoarse - 1) / kBisectCoarse;
+                int kl = 1, kh = K;  // first coarse boundary with a count above v
+                while (kl < kh) {
+                    const int km = (kl + kh) / 2;
+                    if (c[min(km * kBisectCoarse - 1, last)] > v) kh = km;
+                    else kl = km + 1;
+                }
+                int a = (kl - 1) * kBisectCoarse - 1;
+                for (int W = kBisectCoarse; W > 1; W >>= 1) {
+                    const int mid = a + W / 2;
+                    if ((mid >= last ? ctop : c[mid]) <= v) a = mid;
+                }
+                lo = min(a + 1, last);
+            }
         }
         LevelWork w;
         w.p = p;

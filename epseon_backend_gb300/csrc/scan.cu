@@ -219,7 +219,7 @@ __device__ __forceinline__ void run_down(const float* __restrict__ tb, int T0, i
 }
 
 template <int THREADS, int TILE, int STAGES>
-__global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, int n_items) {
+__global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, int n_items, int stride) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float2* buf = reinterpret_cast<float2*>(smem_raw);               // STAGES TMA tiles of (w.x, w.y)
     float* conv = reinterpret_cast<float*>(buf + (size_t)STAGES * TILE);  // the converted tile
@@ -251,10 +251,16 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
         // energy blocks highest first: windows (and so the work) grow with
         // the energy, so the longest items of a potential start first
         const int blk = ipp - 1 - item % ipp;
-        const int j = blk * THREADS + tid;
+        // trial energies stride - 1, 2 stride - 1, ... (and the last one):
+        // every one for stride 1, the bisection scan's coarse grid otherwise
+        const int last = b.n_trial - 1;
+        const int n_sel = (b.n_trial + stride - 1) / stride;
+        auto sel = [&](int q) { return min(q * stride + stride - 1, last); };
+        const bool valid = blk * THREADS + tid < n_sel;
+        const int j = sel(blk * THREADS + tid);
         const PotMeta m = b.meta[p];
         if (m.status & EPSCU_STATUS_BAD) {
-            if (j < b.n_trial) b.counts[(int64_t)p * b.n_trial + j] = 0;
+            if (valid) b.counts[(int64_t)p * b.n_trial + j] = 0;
             continue;  // uniform across the CTA
         }
         // the item's window: union of the decay windows of its energy blocks
@@ -262,8 +268,8 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
         int j0 = m.i0, j1 = m.i1;
         if (b.scan_win) {
             const int nb = (b.n_trial + kScanWinBlock - 1) / kScanWinBlock;
-            const int e0 = blk * THREADS;
-            const int q0 = e0 / kScanWinBlock, q1 = min(nb - 1, (e0 + THREADS - 1) / kScanWinBlock);
+            const int q0 = sel(blk * THREADS) / kScanWinBlock;
+            const int q1 = min(nb - 1, sel(min(blk * THREADS + THREADS, n_sel) - 1) / kScanWinBlock);
             j0 = m.i1;
             j1 = m.i0;
             for (int q = q0; q <= q1; ++q) {
@@ -276,7 +282,7 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
         }
         const TileSeq seq = make_seq(j0, j1, m.k_scan, TILE);
         if (tid == 0) {
-            const int n_e = min(THREADS, b.n_trial - blk * THREADS);
+            const int n_e = min(THREADS, n_sel - blk * THREADS);
             atomicAdd(&b.hdr->scan_updates, (unsigned long long)n_e * (unsigned long long)(j1 - j0));
         }
         const int L = seq.size();
@@ -293,10 +299,11 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
             }
         }
 
-        const double E = trial_energy(m, min(j, b.n_trial - 1));
+        const double E = trial_energy(m, j);
         const double aE = __dmul_rn(m.a, E);
-        // the item's reference energy (middle of its block) and this thread's offset
-        const float H = __double2float_rn(__dmul_rn(m.a, trial_energy(m, min(blk * THREADS + THREADS / 2, b.n_trial - 1))));
+        // the item's reference energy (middle of its block) and this thread's
+        // offset (at most THREADS / 2 strides of trial spacings)
+        const float H = __double2float_rn(__dmul_rn(m.a, trial_energy(m, sel(blk * THREADS + THREADS / 2))));
         const float l = __double2float_rn(aE - (double)H);
         const int k = m.k_scan;
         float A = 1.0f, D = 1.0f;  // u_{j0} = 1, u_{j0-1} = 0
@@ -364,7 +371,7 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
         const double AC = uA * vC;
         const double num = -12.0 * Tk * AC + fk * ((double)Do * vC + (double)D * uA);
         nodes += (num < 0.0) != (AC < 0.0);
-        if (j < b.n_trial) b.counts[(int64_t)p * b.n_trial + j] = nodes;
+        if (valid) b.counts[(int64_t)p * b.n_trial + j] = nodes;
     }
     __syncthreads();
     if (s_abort && tid == 0) {
@@ -373,9 +380,193 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
     }
 }
 
+// ------------------------------------------------------------ bisection scan
+// The levels' brackets need the count only where it changes: the counts at
+// every kBisectCoarse-th trial energy (and the last), then, round by round,
+// at the midpoint of every cell whose end counts differ, until those cells
+// are one trial spacing wide.  That is the bracket the full scan gives (the
+// count is monotone in the energy), from ~128 + 6 (levels) counts per
+// potential instead of n_trial.  counts[] holds -1 where no count was taken.
+
+// The trial indices of the next round (W = 0: the coarse boundaries; else
+// the midpoints of the cells of width W whose end counts differ).  One CTA
+// per potential.
+__global__ void __launch_bounds__(256) bisect_plan_kernel(DevBatch b, int W) {
+    __shared__ int s_n;
+    const int p = blockIdx.x;
+    const PotMeta m = b.meta[p];
+    if (threadIdx.x == 0) s_n = 0;
+    __syncthreads();
+    int32_t* list = b.bis_list + (int64_t)p * b.n_trial;
+    const int32_t* c = b.counts + (int64_t)p * b.n_trial;
+    const int last = b.n_trial - 1;
+    if (!(m.status & EPSCU_STATUS_BAD)) {
+        if (W == 0) {
+            const int K = (b.n_trial + kBisectCoarse - 1) / kBisectCoarse;
+            for (int k = 1 + threadIdx.x; k <= K; k += blockDim.x) list[atomicAdd(&s_n, 1)] = min(k * kBisectCoarse - 1, last);
+        } else {
+            const int ncell = (b.n_trial + W - 1) / W;
+            for (int t = threadIdx.x; t < ncell; t += blockDim.x) {
+                const int a = t * W - 1;  // cell (a, a + W], count(-1) = 0
+                const int ca = a < 0 ? 0 : c[a];
+                const int cb = c[min(a + W, last)];
+                const int mid = a + W / 2;
+                if (ca >= 0 && cb > ca && mid < last) list[atomicAdd(&s_n, 1)] = mid;
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) b.bis_n[p] = s_n;
+}
+
+// Counts at the listed trial energies of each potential: one CTA per
+// potential (longest grids first), up to kCountThreads energies at a time,
+// each thread one energy through the FP32 difference form with
+// T = (aE_hi - W_hi) + (aE_lo - W_lo) (three FADDs: the energies of a round
+// spread over the whole spectrum, so no shared reference energy), on tiles
+// of the window of the chunk's highest energy staged in shared memory.
+constexpr int kCountThreads = 128;
+constexpr int kCountTile = 2048;
+constexpr int kCountSplit = 4;  // CTAs per potential (chunks of energies in parallel)
+
+// the three-FADD step on a raw (w.x, w.y) tile: per point, with the node
+// count; and with the sign history (16-step chunks, popcounted)
+__device__ __forceinline__ void step32t(float aEh, float aEl, float2 w, float& A, float& D, int& nodes) {
+    const float T = (aEh - w.x) + (aEl - w.y);
+    const float X = fmaf(-12.0f, A, D);
+    D = fmaf(T, X, D);
+    const float An = A + fmaf(T, A, D);
+    nodes += (__float_as_uint(An) ^ __float_as_uint(A)) >> 31;
+    A = An;
+}
+
+__device__ __forceinline__ void step32tb(float aEh, float aEl, float wx, float wy, float& A, float& D, uint32_t& bits) {
+    const float T = (aEh - wx) + (aEl - wy);
+    const float X = fmaf(-12.0f, A, D);
+    D = fmaf(T, X, D);
+    A = A + fmaf(T, A, D);
+    bits = __funnelshift_l(__float_as_uint(A), bits, 1);
+}
+
+// points a0..a1 ascending (a0 <= a1) of a raw tile tb whose first point is T0
+__device__ __forceinline__ void run_up_raw(const float2* __restrict__ tb, int T0, int a0, int a1, float aEh, float aEl,
+                                           float& A, float& D, int& nodes) {
+    int i = a0;
+    for (; i <= a1 && (i & 15); ++i) step32t(aEh, aEl, tb[i - T0], A, D, nodes);
+    renorm_f(A, D);
+    uint32_t bits = __float_as_uint(A) >> 31;
+    for (; i + 15 <= a1; i += 16) {
+        const float4* q4 = reinterpret_cast<const float4*>(tb + (i - T0));
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const float4 q = q4[u];
+            step32tb(aEh, aEl, q.x, q.y, A, D, bits);
+            step32tb(aEh, aEl, q.z, q.w, A, D, bits);
+        }
+        flush_bits(bits, nodes);
+        renorm_f(A, D);
+    }
+    for (; i <= a1; ++i) step32t(aEh, aEl, tb[i - T0], A, D, nodes);
+}
+
+// points a0..a1 descending (a0 >= a1)
+__device__ __forceinline__ void run_down_raw(const float2* __restrict__ tb, int T0, int a0, int a1, float aEh,
+                                             float aEl, float& A, float& D, int& nodes) {
+    int i = a0;
+    for (; i >= a1 && ((i & 15) != 15); --i) step32t(aEh, aEl, tb[i - T0], A, D, nodes);
+    renorm_f(A, D);
+    uint32_t bits = __float_as_uint(A) >> 31;
+    for (; i - 15 >= a1; i -= 16) {
+        const float4* q4 = reinterpret_cast<const float4*>(tb + (i - 15 - T0));
+#pragma unroll
+        for (int u = 7; u >= 0; --u) {
+            const float4 q = q4[u];
+            step32tb(aEh, aEl, q.z, q.w, A, D, bits);
+            step32tb(aEh, aEl, q.x, q.y, A, D, bits);
+        }
+        flush_bits(bits, nodes);
+        renorm_f(A, D);
+    }
+    for (; i >= a1; --i) step32t(aEh, aEl, tb[i - T0], A, D, nodes);
+}
+
+__global__ void __launch_bounds__(kCountThreads) count_list_kernel(DevBatch b) {
+    __shared__ __align__(16) float2 tile[kCountTile];
+    __shared__ int s_jmax;
+    const int tid = threadIdx.x;
+    const int p = b.order[blockIdx.x];
+    const PotMeta m = b.meta[p];
+    const int ne = b.bis_n[p];
+    if (ne <= 0 || (m.status & EPSCU_STATUS_BAD)) return;
+    const int32_t* list = b.bis_list + (int64_t)p * b.n_trial;
+    const float2* src = b.Wf2 + m.offf;  // padded to whole tiles
+    const int k = m.k_scan;
+    // chunks of kCountThreads energies, spread over gridDim.y CTAs
+    for (int c0 = blockIdx.y * kCountThreads; c0 < ne; c0 += gridDim.y * kCountThreads) {
+        const int q = c0 + tid;
+        const int j = q < ne ? list[q] : -1;
+        if (tid == 0) s_jmax = -1;
+        __syncthreads();
+        if (j >= 0) atomicMax(&s_jmax, j);
+        __syncthreads();
+        const int jmax = s_jmax;
+        // the window of the chunk's highest energy holds the others'
+        int j0 = m.i0, j1 = m.i1;
+        if (b.scan_win) {
+            const int nb = (b.n_trial + kScanWinBlock - 1) / kScanWinBlock;
+            const int2 wq = b.scan_win[(int64_t)p * nb + jmax / kScanWinBlock];
+            j0 = min(wq.x, k);
+            j1 = max(wq.y, k);
+        }
+        if (tid == 0)
+            atomicAdd(&b.hdr->scan_updates,
+                      (unsigned long long)min(kCountThreads, ne - c0) * (unsigned long long)(j1 - j0));
+        const double aE = __dmul_rn(m.a, trial_energy(m, max(j, 0)));
+        const float aEh = __double2float_rn(aE);
+        const float aEl = __double2float_rn(aE - (double)aEh);
+        float A = 1.0f, D = 1.0f;  // u_{j0} = 1, u_{j0-1} = 0
+        float Ao = 1.0f, Do = 1.0f;
+        int nodes = 0;
+        bool inward = false;
+        const TileSeq seq = make_seq(j0, j1, k, kCountTile);
+        for (int t = 0; t < seq.size(); ++t) {
+            const int T0 = seq.tile(t) * kCountTile;
+            __syncthreads();  // the previous tile is consumed
+            for (int x = tid; x < kCountTile; x += kCountThreads) tile[x] = src[T0 + x];
+            __syncthreads();
+            if (t < seq.n_out) {
+                run_up_raw(tile, T0, max(j0, T0), min(k - 1, T0 + kCountTile - 1), aEh, aEl, A, D, nodes);
+            } else {
+                if (!inward) {
+                    inward = true;
+                    Ao = A;
+                    Do = D;
+                    A = 1.0f;  // v_{j1} = 1, v_{j1+1} = 0
+                    D = 1.0f;
+                }
+                run_down_raw(tile, T0, min(j1, T0 + kCountTile - 1), max(k + 1, T0), aEh, aEl, A, D, nodes);
+            }
+        }
+        if (!inward) {  // no inward tiles: k == j1
+            Ao = A;
+            Do = D;
+            A = 1.0f;
+            D = 1.0f;
+        }
+        // twist pivot sign in FP64: -12 T_k u_k v_k + f_k (D_o v_k + D_i u_k)
+        const double Tk = aE - b.W64[m.off + k];
+        const double fk = 1.0 + Tk;
+        const double uA = (double)Ao, vC = (double)A;
+        const double AC = uA * vC;
+        const double num = -12.0 * Tk * AC + fk * ((double)Do * vC + (double)D * uA);
+        nodes += (num < 0.0) != (AC < 0.0);
+        if (j >= 0) b.counts[(int64_t)p * b.n_trial + j] = nodes;
+    }
+}
+
 template <int THREADS, int TILE, int STAGES>
-void launch_scan32_t(const DevBatch& b, int ctas_per_sm, int sm_count, cudaStream_t s) {
-    const int ipp = (b.n_trial + THREADS - 1) / THREADS;
+void launch_scan32_t(const DevBatch& b, int ctas_per_sm, int sm_count, cudaStream_t s, int stride) {
+    const int ipp = ((b.n_trial + stride - 1) / stride + THREADS - 1) / THREADS;
     const int n_items = ipp * b.n;
     const size_t smem = (size_t)TILE * STAGES * sizeof(float2) + (size_t)TILE * sizeof(float);
     auto kern = scan32_kernel<THREADS, TILE, STAGES>;
@@ -387,7 +578,7 @@ void launch_scan32_t(const DevBatch& b, int ctas_per_sm, int sm_count, cudaStrea
     int grid = sm_count * ctas_per_sm;
     if (grid > n_items) grid = n_items;
     if (grid < 1) grid = 1;
-    kern<<<grid, THREADS, smem, s>>>(b, ipp, n_items);
+    kern<<<grid, THREADS, smem, s>>>(b, ipp, n_items, stride);
 }
 
 template <int THREADS, int TILE, int STAGES>
@@ -418,10 +609,20 @@ void launch_scan64(const DevBatch& b, cudaStream_t s) {
 
 int scan32_max_tile() { return 4096; }
 
-void launch_scan32(const DevBatch& b, const ScanShape& sh, int sm_count, cudaStream_t s) {
+void launch_bisect_scan(const DevBatch& b, const ScanShape& sh, int sm_count, cudaStream_t s) {
+    cudaMemsetAsync(b.counts, 0xff, sizeof(int32_t) * (size_t)b.n * b.n_trial, s);  // -1: no count taken
+    // the coarse grid with the throughput scan, then the bisection rounds
+    launch_scan32(b, sh, sm_count, s, kBisectCoarse);
+    for (int W = kBisectCoarse; W > 1; W /= 2) {
+        bisect_plan_kernel<<<b.n, 256, 0, s>>>(b, W);
+        count_list_kernel<<<dim3(b.n, kCountSplit), kCountThreads, 0, s>>>(b);
+    }
+}
+
+void launch_scan32(const DevBatch& b, const ScanShape& sh, int sm_count, cudaStream_t s, int stride) {
 #define EPSCU_SCAN32_CASE(TH, TI, ST)                                              \
     if (sh.threads == TH && sh.tile == TI && sh.stages == ST) {                    \
-        launch_scan32_t<TH, TI, ST>(b, sh.ctas_per_sm, sm_count, s);               \
+        launch_scan32_t<TH, TI, ST>(b, sh.ctas_per_sm, sm_count, s, stride);       \
         return;                                                                    \
     }
     EPSCU_SCAN32_CASE(128, 1024, 2)
@@ -435,7 +636,7 @@ void launch_scan32(const DevBatch& b, const ScanShape& sh, int sm_count, cudaStr
     EPSCU_SCAN32_CASE(512, 1024, 4)
     EPSCU_SCAN32_CASE(512, 2048, 3)
 #undef EPSCU_SCAN32_CASE
-    launch_scan32_t<256, 2048, 3>(b, sh.ctas_per_sm, sm_count, s);
+    launch_scan32_t<256, 2048, 3>(b, sh.ctas_per_sm, sm_count, s, stride);
 }
 
 }  // namespace epscu

@@ -96,3 +96,27 @@ def test_psi_buffer_too_small(ctx, method):
     # the context stays usable
     sol = ctx.solve([V], r0, r1, mu, cap, 1024, method=method, level_capacity=64)
     assert sol.n_out[0] > 0
+
+
+def test_bisection_scan_batch(ctx):
+    """A batch large enough for the bisection scan (counts only where they
+    change: the coarse grid of every 8th trial energy, then halved cells)
+    gives every level of the plain FP64 solver (itself bit-exact with the
+    oracle) within the fast method's tolerance, with its node count."""
+    b = synth.mixed_batch(B=640, n_min=2048, n_max=6144, seed=11)
+    b.n_trial = 2048
+    Vs = b.potentials()
+    ref = ctx.solve(Vs, b.r_min, b.r_max, b.mu, b.e_cap, b.n_trial, method=capi.METHOD_PLAIN_FP64, level_capacity=256)
+    sol = ctx.solve(Vs, b.r_min, b.r_max, b.mu, b.e_cap, b.n_trial, method=capi.METHOD_FAST_FP32C, level_capacity=256)
+    assert np.array_equal(sol.n_total, ref.n_total)
+    assert np.array_equal(sol.n_out, ref.n_out)
+    checked = 0
+    for q in range(len(b)):
+        n = sol.n_out[q]
+        if n == 0:
+            continue
+        if not (ref.status[q, 0] & capi.LEVEL_UNDER_RESOLVED):
+            assert np.array_equal(sol.nodes[q, :n], ref.nodes[q, :n])
+        assert np.max(np.abs(sol.energy[q, :n] - ref.energy[q, :n])) < E_TOL[capi.METHOD_FAST_FP32C]
+        checked += n
+    assert checked > 10000

@@ -4,7 +4,7 @@ The fast method's scan and per-level passes run on a window [j0, j1] of the
 grid instead of the oracle's [i0, i1]: beyond the classical turning points of
 an energy E_up the discrete solution decays at least by acosh(1 + 6 t_i) per
 step (t_i = a (V_i - E_up)), and the window ends where that exponent, summed
-from the turning point, reaches 46.  This file restates the kernels' rule in
+from the turning point, reaches 36.  This file restates the kernels' rule in
 numpy (in FP64; the kernels sum it in FP32 with block minima rounded down) and
 checks on dense eigen-decompositions of the discrete problem that the cut
 leaves every eigenvalue below E_up unchanged to FP64 rounding and the
@@ -19,7 +19,7 @@ import pytest
 from epseon_backend_gb300 import synth
 from oracle import oracle as O
 
-DECAY = 46.0
+DECAY = 36.0
 
 
 def decay_window(V, g, mu, Eu, decay=DECAY):
