@@ -42,6 +42,10 @@ CPU_SAMPLE = 96  # potentials of the workload the CPU legs time
 # dram__bytes_read.sum + dram__bytes_write.sum of one scan32 launch per grid
 # point, ncu on the 128-potential mixed batch (18.12 MB / 2,242,300 points)
 SCAN32_DRAM_BYTES_PER_POINT = 8.08
+# ncu (dram__bytes_read.sum + dram__bytes_write.sum) of refine_long_kernel per
+# algorithmic point-update on the 512-potential mixed batch (54.70 MB over
+# 147,450,449 point-updates: the windows' W is re-read from L2)
+REFINE_LONG_DRAM_BYTES_PER_UPDATE = 0.371
 
 
 def dist_env():
@@ -405,21 +409,33 @@ def main():
                "sample": f"{len(idx)} of {len(b)} potentials (seeded random), plain FP64 method, {dt:.1f} s",
                "plain_gpu_bit_exact_on_sample": bool(same)}
 
-    # ---- roofline of the dominant kernel: scan32 (the longest single launch;
-    # the per-level stages are split over several kernels each).  Unit: one
-    # Numerov point-update = 9 algorithmic flops (T, f, g, two-term recurrence);
-    # compensation, renormalisation and sign bookkeeping are not counted.
-    scan_flops = 9.0 * st.scan_point_updates
-    ach = scan_flops / (st.ms_scan * 1e-3) / 1e12
-    # DRAM bytes per launch: ncu measured SCAN32_DRAM_BYTES_PER_POINT on the
-    # 128-potential mixed batch (the potential read once; tiles re-read from
-    # L2 and shared memory), scaled by the grid points of this workload
-    traffic = SCAN32_DRAM_BYTES_PER_POINT * float(b.N.sum())
+    # ---- roofline of the dominant kernel: refine_long_kernel, the longest
+    # single launch of the step (the long levels' CTA-per-level refinement;
+    # time from its own events in the stage-timed solve, on the solve stream).
+    # Unit: one Numerov point-update = 9 algorithmic flops (T, f, g, two-term
+    # recurrence) in its FP32 and its double-float passes alike; the chunked
+    # three-phase passes, the compensation (a double-float step issues ~10x
+    # the FP32 instructions), renormalisation and sign bookkeeping are not
+    # counted, so the fraction is structurally far below 1.
+    rl_updates = int(st.long_fp32_point_updates + st.long_df_point_updates)
+    ach = 9.0 * rl_updates / (st.ms_refine_long * 1e-3) / 1e12 if st.ms_refine_long > 0 else 0.0
+    traffic = (REFINE_LONG_DRAM_BYTES_PER_UPDATE * rl_updates) if REFINE_LONG_DRAM_BYTES_PER_UPDATE else None
     roof = {"bound": "fp32_alu", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s", "frac": ach / fp32_peak,
-            "traffic": traffic, "traffic_unit": "bytes per launch (ncu-measured per-point DRAM bytes x points)",
-            "kernel": "scan32_kernel",
-            "algorithmic": {"point_updates": int(st.scan_point_updates), "flops_per_update": 9},
+            "traffic": traffic,
+            "traffic_unit": "bytes per launch (ncu-measured DRAM bytes per point-update x point-updates)",
+            "kernel": "refine_long_kernel", "ms": st.ms_refine_long,
+            "algorithmic": {"point_updates": rl_updates, "fp32_pass_point_updates": int(st.long_fp32_point_updates),
+                            "double_float_pass_point_updates": int(st.long_df_point_updates),
+                            "flops_per_update": 9},
             "peak_source": "measured FP32 FMA burst (epscu_measure_fma_peaks), 2 flops per FMA"}
+    # the scan stage in the same unit (the coarse scan32 launch plus, on large
+    # batches, the bisection rounds; scan32 alone is FP32-issue-bound)
+    scan_ach = 9.0 * st.scan_point_updates / (st.ms_scan * 1e-3) / 1e12
+    roof_scan = {"kernel": "scan stage (scan32_kernel" + (" on every 8th trial energy + bisection rounds)"
+                                                          if len(b) >= 512 else ")"),
+                 "achieved": scan_ach, "peak": fp32_peak, "unit": "TFLOP/s", "frac": scan_ach / fp32_peak,
+                 "ms": st.ms_scan, "point_updates": int(st.scan_point_updates),
+                 "dram_bytes_per_grid_point_scan32": SCAN32_DRAM_BYTES_PER_POINT}
     # the per-level stages in the same unit (algorithmic point-updates counted
     # by the kernels over the level windows; latency-bound lane marches)
     stage_rates = {
@@ -473,6 +489,7 @@ def main():
                       "refine_max_level_updates": st.refine_max_level_updates,
                       "df_max_level_updates": st.df_max_level_updates},
         "roofline": roof,
+        "roofline_scan": roof_scan,
         "roofline_plain_fp64": roof_plain,
         "stage_rates": stage_rates,
         "psi_write": {"bytes": st.psi_bytes, "GB_per_s": write_gbs, "hbm_peak_GBs": hbm},

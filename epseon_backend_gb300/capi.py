@@ -113,6 +113,10 @@ class Stats(C.Structure):
         ("df_max_level_updates", C.c_int64),
         ("refine_max_iters", C.c_int32),
         ("reserved", C.c_int32),
+        ("ms_refine_long", C.c_float),
+        ("reserved2", C.c_int32),
+        ("long_fp32_point_updates", C.c_int64),
+        ("long_df_point_updates", C.c_int64),
     ]
 
 

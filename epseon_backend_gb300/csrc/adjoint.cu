@@ -21,29 +21,24 @@ namespace {
 
 // psi rows of the last solve in place (row s of potential p at psi_off + s N);
 // accumulate = add into dL_dV instead of storing.  One CTA per (potential,
-// kAdjPoints points), four points per thread (a stride of the CTA's width
-// apart, so every load is coalesced); the CTA first narrows the level loop to
-// the levels whose window meets its points (windows grow with the level, so
-// near the ends of a grid only the highest levels remain) and stages their
-// windows and dL/dE in shared memory.  Per level the four points' loads are
-// in flight together (the kernel is bound by HBM latency with one).
-constexpr int kAdjThreads = 256;
-constexpr int kAdjPer = 4;
-constexpr int kAdjPoints = kAdjThreads * kAdjPer;
+// 256 points); the CTA first narrows the level loop to the levels whose
+// window meets its points (windows grow with the level, so near the ends of
+// a grid only the highest levels remain), stages their windows and dL/dE in
+// shared memory, and reads four rows per step (four loads in flight per
+// thread: the kernel is bound by HBM latency otherwise).
 constexpr int kAdjTile = 256;  // levels staged per round
 
-__global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(DevBatch b, const double* __restrict__ gE,
-                                                              double* __restrict__ gV,
-                                                              const int64_t* __restrict__ offsets,
-                                                              const double* __restrict__ psi, int accumulate) {
+__global__ void __launch_bounds__(256) adjoint_kernel(DevBatch b, const double* __restrict__ gE, double* __restrict__ gV,
+                                                      const int64_t* __restrict__ offsets, const double* __restrict__ psi,
+                                                      int accumulate) {
     __shared__ int s_lo, s_hi;
     __shared__ int2 s_win[kAdjTile];
     __shared__ double s_g[kAdjTile];
     const int p = blockIdx.y;
     const PotMeta m = b.meta[p];
-    const int i_a = blockIdx.x * kAdjPoints;
+    const int i_a = blockIdx.x * blockDim.x;
     if (i_a >= m.N) return;
-    const int i_b = min(i_a + kAdjPoints, m.N) - 1;
+    const int i_b = min(i_a + (int)blockDim.x, m.N) - 1;
     const LevelWork* lw = b.levels + m.level_base;
     if (threadIdx.x == 0) {
         s_lo = m.n_out;
@@ -58,10 +53,10 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(DevBatch b, const 
     }
     __syncthreads();
     const int lo = s_lo, hi = s_hi;
-    const int i0 = i_a + threadIdx.x;  // this thread's points: i0 + u kAdjThreads
-    const double* rows = psi + m.psi_off + i0;
+    const int i = i_a + threadIdx.x;
+    const double* rows = psi + m.psi_off + i;
     const double* g = gE + (int64_t)p * b.level_capacity;
-    double acc[kAdjPer] = {};
+    double acc = 0.0;
     for (int t0 = lo; t0 <= hi; t0 += kAdjTile) {
         const int nt = min(kAdjTile, hi - t0 + 1);
         __syncthreads();  // the previous round's stage is consumed
@@ -70,33 +65,29 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(DevBatch b, const 
             s_g[q] = g[t0 + q];
         }
         __syncthreads();
-        for (int q = 0; q < nt; ++q) {
-            const int2 wq = s_win[q];
-            const double gq = s_g[q];
-            const double* row = rows + (int64_t)(t0 + q) * m.N;
-            double v[kAdjPer];
-#pragma unroll
-            for (int u = 0; u < kAdjPer; ++u) {
-                const int i = i0 + u * kAdjThreads;
-                v[u] = (i <= i_b && i >= wq.x && i <= wq.y) ? __ldg(row + u * kAdjThreads) : 0.0;
-            }
-            // a level's term is added only inside its window, as if the loop
-            // skipped the others (a non-finite dL/dE stays out of their sums)
-#pragma unroll
-            for (int u = 0; u < kAdjPer; ++u) {
-                const int i = i0 + u * kAdjThreads;
-                acc[u] = (i >= wq.x && i <= wq.y) ? fma(gq * v[u], v[u], acc[u]) : acc[u];
-            }
-        }
-    }
-#pragma unroll
-    for (int u = 0; u < kAdjPer; ++u) {
-        const int i = i0 + u * kAdjThreads;
         if (i > i_b) continue;
-        const double x = acc[u] * m.h;
-        if (accumulate) gV[offsets[p] + i] += x;
-        else gV[offsets[p] + i] = x;
+        // (a level's term is added only inside its window, as if the loop
+        // skipped the others: a non-finite dL/dE stays out of their sums)
+        auto inside = [&](int q) {
+            const int2 wq = s_win[q];
+            return i >= wq.x && i <= wq.y;
+        };
+        auto load = [&](int q) { return inside(q) ? __ldg(rows + (int64_t)(t0 + q) * m.N) : 0.0; };
+        auto add = [&](int q, double v) { acc = inside(q) ? fma(s_g[q] * v, v, acc) : acc; };
+        int q = 0;
+        for (; q + 3 < nt; q += 4) {
+            const double v0 = load(q), v1 = load(q + 1), v2 = load(q + 2), v3 = load(q + 3);
+            add(q, v0);
+            add(q + 1, v1);
+            add(q + 2, v2);
+            add(q + 3, v3);
+        }
+        for (; q < nt; ++q) add(q, load(q));
     }
+    if (i > i_b) return;
+    acc *= m.h;
+    if (accumulate) gV[offsets[p] + i] += acc;
+    else gV[offsets[p] + i] = acc;
 }
 
 // Explicit layout (stateless adjoint): per-potential arrays on the device.
@@ -133,9 +124,9 @@ void launch_adjoint(const DevBatch& b, const double* dL_dE, double* dL_dV, int64
     (void)total_points;
     (void)recompute;
     (void)sm_count;
-    // grid.x covers the longest grid; CTAs past a shorter grid exit at once
-    dim3 grid((b.max_N + kAdjPoints - 1) / kAdjPoints, b.n);
-    adjoint_kernel<<<grid, kAdjThreads, 0, s>>>(b, dL_dE, dL_dV, offsets_dev, b.psi, 0);
+    // grid.x covers the longest grid; threads past a shorter grid exit at once
+    dim3 grid((b.max_N + 255) / 256, b.n);
+    adjoint_kernel<<<grid, 256, 0, s>>>(b, dL_dE, dL_dV, offsets_dev, b.psi, 0);
 }
 
 }  // namespace epscu

@@ -71,7 +71,7 @@ struct Header {
     int32_t fallbacks;      // levels that needed the bisection fallback
     int32_t n_units;        // warp work units (<= 32 levels of one potential)
     int32_t n_twist;        // levels handed to the twist-index search
-    int32_t queue[8];       // work-queue heads of the per-level kernels
+    int32_t queue[12];      // work-queue heads of the per-level kernels
     int32_t n_long;         // levels whose window takes the CTA-per-level passes
     int32_t n_redo;         // norm passes redone at E + dE
     unsigned long long scan_updates;    // point-updates the windowed FP32 scan performed
@@ -82,10 +82,13 @@ struct Header {
     unsigned long long df_max_updates;      // largest per-level point-updates of newton_df / norm_df
     int32_t refine_max_iters;               // most refine32 passes of one level
     int32_t pad_hdr;
+    unsigned long long long32_updates;      // refine_long (long list): FP32 pass point-updates
+    unsigned long long longdf_updates;      //   and double-float pass point-updates
 };
 
 // queue ids of the per-level kernels
-enum { kQRefine32 = 0, kQNewtonDF, kQNormDF, kQWriteDF, kQBisect64, kQNorm64, kQWrite64 };
+enum { kQRefine32 = 0, kQNewtonDF, kQNormDF, kQWriteDF, kQBisect64, kQNorm64, kQWrite64, kQLongRefine, kQFallback,
+       kQNormLong, kQTwistLong };
 
 // internal level flags (not reported: gather keeps the public bits only)
 // the Newton stage handed the level to the fallback

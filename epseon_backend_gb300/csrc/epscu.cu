@@ -58,7 +58,7 @@ struct DevBuf {
     size_t cap = 0;
 };
 
-constexpr int kStageEvents = 8;
+constexpr int kStageEvents = 10;  // 0-6 stages, 6-7 autotune, 8-9 around refine_long
 
 }  // namespace
 
@@ -343,7 +343,9 @@ void enqueue_pipeline(epscu_ctx* ctx, const DevBatch& b, int method, bool want_p
         } else {
             // stage timing: one stream, stages in sequence
             launch_refine32(b, ctx->sm_count, s);
+            rec(8);
             launch_refine_long(b, ctx->sm_count, s);
+            rec(9);
             rec(3);
             launch_newton_df(b, ctx->sm_count, s);
             launch_fallback_long(b, ctx->sm_count, s);
@@ -701,6 +703,7 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
         }
         st.ms_write = el(4, 5);
         st.ms_total = el(0, 6);
+        if (method == EPSCU_METHOD_FAST_FP32C) st.ms_refine_long = el(8, 9);
     } else {
         cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[6]);
         st.ms_total = ms;
@@ -741,6 +744,8 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
         st.refine_max_level_updates = (int64_t)hh->refine_max_updates;
         st.df_max_level_updates = (int64_t)hh->df_max_updates;
         st.refine_max_iters = hh->refine_max_iters;
+        st.long_fp32_point_updates = (int64_t)hh->long32_updates;
+        st.long_df_point_updates = (int64_t)hh->longdf_updates;
     }
     ctx->stats = st;
 

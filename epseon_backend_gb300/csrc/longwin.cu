@@ -828,7 +828,14 @@ __global__ void __launch_bounds__(kLongThreads) refine_long_kernel(DevBatch b, i
     __shared__ LongShared32 sh32;
     const int n = fallback ? min(b.hdr->fallbacks, b.max_levels) : min(b.hdr->n_long, b.max_levels);
     const int32_t* list = fallback ? b.fallback_list : b.long_list;
-    for (int q = blockIdx.x; q < n; q += gridDim.x) {
+    __shared__ int s_q;
+    // levels from a device queue (a CTA takes the next as it finishes one)
+    for (;;) {
+        if (threadIdx.x == 0) s_q = atomicAdd(&b.hdr->queue[fallback ? kQFallback : kQLongRefine], 1);
+        __syncthreads();
+        const int q = s_q;
+        __syncthreads();  // every thread has read s_q
+        if (q >= n) break;
         const int slot = list[q];
         LevelWork w = b.levels[slot];
         if (w.status & EPSCU_STATUS_NOTFOUND) continue;
@@ -947,6 +954,10 @@ __global__ void __launch_bounds__(kLongThreads) refine_long_kernel(DevBatch b, i
             const unsigned long long pts = (unsigned long long)(w.j1 - w.j0);
             atomicAdd(&b.hdr->refine_updates, (unsigned long long)n_pass32 * pts);
             atomicAdd(&b.hdr->df_updates, (unsigned long long)n_pass * pts);
+            if (!fallback) {
+                atomicAdd(&b.hdr->long32_updates, (unsigned long long)n_pass32 * pts);
+                atomicAdd(&b.hdr->longdf_updates, (unsigned long long)n_pass * pts);
+            }
             b.levels[slot] = w;
         }
         __syncthreads();
@@ -960,7 +971,14 @@ __global__ void __launch_bounds__(kLongThreads) refine_long_kernel(DevBatch b, i
 __global__ void __launch_bounds__(kLongThreads) norm_long_kernel(DevBatch b) {
     __shared__ LongShared sh;
     const int n = min(b.hdr->n_long, b.max_levels);
-    for (int q = blockIdx.x; q < n; q += gridDim.x) {
+    __shared__ int s_q;
+    // levels from a device queue (a CTA takes the next as it finishes one)
+    for (;;) {
+        if (threadIdx.x == 0) s_q = atomicAdd(&b.hdr->queue[kQNormLong], 1);
+        __syncthreads();
+        const int q = s_q;
+        __syncthreads();  // every thread has read s_q
+        if (q >= n) break;
         const int slot = b.long_list[q];
         LevelWork w = b.levels[slot];
         if (w.status & (EPSCU_STATUS_NOTFOUND | EPSCU_STATUS_CANCELLED)) continue;
@@ -1020,7 +1038,14 @@ __global__ void __launch_bounds__(kLongThreads) norm_long_kernel(DevBatch b) {
 __global__ void __launch_bounds__(kLongThreads) twist_long_kernel(DevBatch b) {
     __shared__ LongShared sh;
     const int n = min(b.hdr->n_twist, b.max_twist);
-    for (int q = blockIdx.x; q < n; q += gridDim.x) {
+    __shared__ int s_q;
+    // levels from a device queue (a CTA takes the next as it finishes one)
+    for (;;) {
+        if (threadIdx.x == 0) s_q = atomicAdd(&b.hdr->queue[kQTwistLong], 1);
+        __syncthreads();
+        const int q = s_q;
+        __syncthreads();  // every thread has read s_q
+        if (q >= n) break;
         const int slot = b.twist_list[q];
         LevelWork w = b.levels[slot];
         const PotMeta m = b.meta[w.p];

@@ -229,6 +229,13 @@ typedef struct epscu_stats {
                                       passes on the lane path (fast method) */
     int32_t refine_max_iters;      /* most FP32 refinement passes of one level */
     int32_t reserved;
+    /* the long levels' refinement kernel (CTA per level; fast method): its time
+       (EPSCU_STAGE_TIMING only) and its point-updates in FP32 and double-float
+       passes (algorithmic: one grid point of one pass) */
+    float ms_refine_long;
+    int32_t reserved2;
+    int64_t long_fp32_point_updates;
+    int64_t long_df_point_updates;
 } epscu_stats;
 epscu_status epscu_last_stats(epscu_ctx* ctx, epscu_stats* stats);
 
