@@ -84,17 +84,6 @@ __device__ __forceinline__ int fexp(float x) { return (int)((__float_as_uint(x) 
 // 2^e as a float, |e| <= 125
 __device__ __forceinline__ float fpow2(int e) { return __int_as_float((127 + e) << 23); }
 
-// exact x 2^X as a double, built from the bit pattern (integer pipe, no FP64
-// instruction) while the result stays a normal double; |X| < 900
-__device__ __forceinline__ double f2d_pow2(float x, int X) {
-    const uint32_t u = __float_as_uint(x);
-    const uint32_t ex = (u >> 23) & 0xffu;
-    if (ex == 0u || ex == 0xffu) return (double)x * __hiloint2double((1023 + X) << 20, 0);
-    const uint32_t man = u & 0x7fffffu;
-    const uint32_t hi = (u & 0x80000000u) | ((ex + 896u + (uint32_t)X) << 20) | (man >> 3);
-    return __hiloint2double((int)hi, (int)(man << 29));
-}
-
 // Sum of squares in double-float with an FP64 spill.  The sum is d + x 2^pend
 // in the current scale; add() takes terms, rescale(s) multiplies the whole sum
 // by 2^s (the renormalisation of the state), value() returns it in FP64.  The

@@ -100,7 +100,7 @@ def test_descent_matches_full_scan(n_trial, seed):
         assert taken < n_trial // 3  # far fewer counts than the full scan
 
 
-def test_counts_taken_on_a_spectrum_like_cfg3():
+def test_counts_taken_on_a_mixed_batch_spectrum():
     """~45 levels over 8192 trial energies: the rounds take ~1/6 of the counts."""
     n_trial = 8192
     E = np.cumsum(np.linspace(400, 60, 45))  # a Morse-like ladder in trial units

@@ -1,6 +1,6 @@
 """Parity of the CUDA solver (through the C ABI) with the FP64 oracle.
 
-Tolerances (spec bar): node counts bit-exact; energies within 1e-10
+Tolerances: node counts bit-exact; energies within 1e-10
 Hartree for the plain FP64 method (bit-exact here, same arithmetic as the
 oracle) and 1e-9 for the FP32-compensated method; normalised wavefunctions
 within 1e-8 in L2 (sum (psi - psi_ref)^2 h).
