@@ -17,14 +17,14 @@ namespace epscu {
 // the point-updates in double-float but cut the latency ~80x.  So the
 // threshold falls with the number of levels (fewer lanes to keep the GPU
 // busy): 8192 points at >= ~9e4 levels (the 2048-potential mixed batch),
-// proportionally less below, never under 2048.  Measured on GB300 with the
-// long levels on their own stream beside the lane kernels: the 2048-potential
-// batch (93k levels) is fastest at 8192-12288, the 256-potential bump batch
-// (14k levels) at 4096, the 64-Morse batch (3.4k levels) at 2048.
-// DevBatch::long_window > 0 overrides it.
+// proportionally less below, never under 1024.  Measured on GB300 with the
+// long levels on their own stream beside the lane kernels and FP32 passes on
+// the CTA path: the 2048-potential batch (93k levels) is fastest at 8192, the
+// 256-potential bump batch (14k levels) at 2048, the 64-Morse batch (3.4k
+// levels) at 1024-1536.  DevBatch::long_window > 0 overrides it.
 constexpr int kLongWindow = 8192;
-constexpr int kLongWindowLevels = 45000;
-constexpr int kMinLongWindow = 2048;
+constexpr int kLongWindowLevels = 60000;
+constexpr int kMinLongWindow = 1024;
 
 __host__ __device__ __forceinline__ int default_long_window(int total_levels) {
     int w = kMinLongWindow;

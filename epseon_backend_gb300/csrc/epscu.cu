@@ -7,7 +7,9 @@
 // device-resident solve (replayed when the same buffers are solved again).
 //
 // Solve pipeline:
-//   prepare -> scan (FP64 | FP32 TMA persistent) -> level set-up + brackets
+//   prepare -> scan (FP64 | FP32 TMA persistent; for batches of >= 512
+//   potentials the FP32 scan on every 8th trial energy, then bisection rounds
+//   where the counts change) -> level set-up + brackets
 //   plain : bisect64 -> norm64 -> twist64 -> write64            (native FP64)
 //   fast  : window, then two branches on two streams (graph fork/join):
 //             lane levels: refine32 -> newton_df -> fallback -> norm_df

@@ -4,19 +4,21 @@
 // significands, see dfloat.cuh) in the Blatt difference form
 //     D' = D + T (D - 12 A),   A' = A + (T A + D')
 // with T = aE - W carried as a double-float pair; FP64 is used only for the
-// matching-point difference gamma_k, the Newton step and the norm integral
-// (sum psi^2, accumulated in FP64 every 8 points).  Per grid point this costs
-// ~110 FP32 instructions and at most one FP64 instruction, against ~16 FP64
-// instructions (~1000 FP32-issue equivalents on GB300) for the same pass in
-// native FP64.
+// matching-point difference gamma_k, the Newton step and the rare spill of
+// the norm integral (sum psi^2 in double-float, dfloat.cuh SqSum).  Per grid
+// point this costs ~110 FP32 instructions and no FP64 instruction, against
+// ~16 FP64 instructions (~1000 FP32-issue equivalents on GB300) for the same
+// pass in native FP64.
 //
 //  newton_df : Cooley corrections from the FP32 energy (one or two passes) in
 //              an FP64 count bracket; levels that do not settle go to the
 //              CTA-per-level Newton of longwin.cu (the fallback).
 //  norm_df   : sums, node count, peak of |psi| and the constants of the
 //              write; with psi requested its final pass also stores the
-//              unnormalised psi-hat in the level's row, and
-//  scale_psi : applies the constants (one HBM pass over the rows).
+//              unnormalised psi-hat in the level's row as tagged float pairs
+//              (dfpass.cuh), and
+//  scale_psi : turns them into the normalised doubles (one HBM pass over the
+//              windows, no FP64 instruction per point).
 //  (the twist-index search for the levels norm_df flags is twist_long in
 //  longwin.cu, one CTA per level)
 //  write_df  : recomputes psi from the stored constants (the adjoint's

@@ -17,7 +17,9 @@
 //           once relative to |T| and to the energy offset inside the item, so
 //           the count is reliable to |E - E_v| of a few 1e-9 Hartree.  The
 //           twist pivot is evaluated in FP64 in the cancellation-free form
-//           -12 T_k A C + f_k (D_o C + D_i A).
+//           -12 T_k A C + f_k (D_o C + D_i A).  With a stride it counts only
+//           at every stride-th trial energy (the bisection scan's coarse grid).
+//  bisect_plan + count_list : the bisection rounds (below).
 #include <cuda_runtime.h>
 #include <stdint.h>
 

@@ -103,7 +103,7 @@ typedef struct epscu_opts {
     int32_t tune;        /* 0 = use cached/default launch shape, 1 = autotune */
     int32_t long_window; /* fast method: levels whose window exceeds this many points run
                             their passes one CTA per level (0: chosen from the number of
-                            levels, 2048 - 8192) */
+                            levels, 1024 - 8192) */
 } epscu_opts;
 
 /* Caller-owned outputs.  Level slot s of potential p is p*level_capacity + s
