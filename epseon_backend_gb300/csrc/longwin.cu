@@ -27,15 +27,19 @@
 // product applied to the starting state loses nothing to the discarded
 // subdominant solution.
 //
-// Kernels (one CTA per long level, levels from the long list the window
-// kernel fills; the lane-per-level kernels skip these levels):
-//   refine_long : safeguarded Cooley-Newton in double-float from the scan
-//                 bracket to 1e-12 (replaces refine32 + newton_df); run again
-//                 over the levels newton_df could not settle (the fallback:
-//                 any window length, from the scan bracket widened by one
-//                 trial spacing);
-//   norm_long   : the norm pass and its match-point candidates (as norm_df);
-//   write_long  : psi to HBM (as write_df).
+// Kernels (one CTA per long level, levels taken from a device queue over the
+// long list the window kernel fills; the lane-per-level kernels skip these
+// levels):
+//   refine_long : from the scan bracket, FP32 passes (the same three phases
+//                 in FP32, long_side32) to 2e-9, then double-float
+//                 state-only Newton to 1e-12 (replaces refine32 + newton_df);
+//                 run again over the levels newton_df could not settle (the
+//                 fallback: any window length, full double-float passes from
+//                 the scan bracket widened by one trial spacing);
+//   norm_long   : the norm pass and its match-point candidates (as norm_df),
+//                 storing psi-hat as tagged float pairs for scale_psi;
+//   twist_long  : the twist-index search for the levels the norm passes flag;
+//   write_long  : psi from the final constants (the adjoint's recompute path).
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
