@@ -731,7 +731,7 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     // (refine_long over the fallback list), norm_df, norm_long, twist_long,
     // gather (+ zero_psi, scale_psi)
     const bool psi_kernels = want_psi || keep_psi;
-    st.kernel_launches = method == EPSCU_METHOD_FAST_FP32C ? 16 + (psi_kernels ? 2 : 0) : 9 + (psi_kernels ? 1 : 0);
+    st.kernel_launches = method == EPSCU_METHOD_FAST_FP32C ? 15 + (psi_kernels ? 2 : 0) : 9 + (psi_kernels ? 1 : 0);
     if (b.bis_list) st.kernel_launches += 6;  // three plan + count rounds after the coarse scan32
     if (method == EPSCU_METHOD_PLAIN_FP64) {
         st.refine_point_updates = 0;
