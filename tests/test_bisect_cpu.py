@@ -109,3 +109,21 @@ def test_counts_taken_on_a_mixed_batch_spectrum():
     assert np.sum(c >= 0) < n_trial // 6
     for v in range(int(full[-1])):
         assert descend(c, v) == full_search(full, v)
+
+
+def test_descent_on_oracle_counts():
+    """The FP64 oracle's scan counts of real potentials (Morse, LJ, bumps):
+    the bisection rounds and the descent give the full scan's bracket of
+    every level."""
+    from epseon_backend_gb300 import synth
+    from oracle import oracle as O
+
+    b = synth.mixed_batch(B=6, n_min=2048, n_max=4096, n_trial=1000, seed=13)
+    Vs = [b.V(i) for i in range(len(b))]
+    refs = O.solve_batch(Vs, b.r_min, b.r_max, b.mu, b.e_cap, b.n_trial)
+    for ref in refs:
+        full = np.asarray(ref.counts, np.int64)
+        assert full.size == b.n_trial and np.all(np.diff(full) >= 0)
+        c = rounds(full)
+        for v in range(int(full[-1])):
+            assert descend(c, v) == full_search(full, v)
