@@ -492,10 +492,21 @@ __device__ __forceinline__ void run_down_raw(const float2* __restrict__ tb, int 
     for (; i >= a1; --i) step32t(aEh, aEl, tb[i - T0], A, D, nodes);
 }
 
+// Two threads per listed energy: warps 0-1 march the outward side, warps 2-3
+// the inward side of the same kCountEnergies energies, on their own tiles,
+// so a round waits for half of the longest window's serial march; the inward
+// half hands its state to the outward one for the twist pivot.
+constexpr int kCountEnergies = kCountThreads / 2;
+
 __global__ void __launch_bounds__(kCountThreads) count_list_kernel(DevBatch b) {
-    __shared__ __align__(16) float2 tile[kCountTile];
+    __shared__ __align__(16) float2 tile_o[kCountTile];
+    __shared__ __align__(16) float2 tile_i[kCountTile];
+    __shared__ float s_A[kCountEnergies], s_D[kCountEnergies];
+    __shared__ int s_nodes[kCountEnergies];
     __shared__ int s_jmax;
     const int tid = threadIdx.x;
+    const int side = tid / kCountEnergies;  // 0: outward, 1: inward (warp-uniform)
+    const int e = tid - side * kCountEnergies;
     const int p = b.order[blockIdx.x];
     const PotMeta m = b.meta[p];
     const int ne = b.bis_n[p];
@@ -503,9 +514,9 @@ __global__ void __launch_bounds__(kCountThreads) count_list_kernel(DevBatch b) {
     const int32_t* list = b.bis_list + (int64_t)p * b.n_trial;
     const float2* src = b.Wf2 + m.offf;  // padded to whole tiles
     const int k = m.k_scan;
-    // chunks of kCountThreads energies, spread over gridDim.y CTAs
-    for (int c0 = blockIdx.y * kCountThreads; c0 < ne; c0 += gridDim.y * kCountThreads) {
-        const int q = c0 + tid;
+    // chunks of kCountEnergies energies, spread over gridDim.y CTAs
+    for (int c0 = blockIdx.y * kCountEnergies; c0 < ne; c0 += gridDim.y * kCountEnergies) {
+        const int q = c0 + e;
         const int j = q < ne ? list[q] : -1;
         if (tid == 0) s_jmax = -1;
         __syncthreads();
@@ -522,47 +533,47 @@ __global__ void __launch_bounds__(kCountThreads) count_list_kernel(DevBatch b) {
         }
         if (tid == 0)
             atomicAdd(&b.hdr->scan_updates,
-                      (unsigned long long)min(kCountThreads, ne - c0) * (unsigned long long)(j1 - j0));
+                      (unsigned long long)min(kCountEnergies, ne - c0) * (unsigned long long)(j1 - j0));
         const double aE = __dmul_rn(m.a, trial_energy(m, max(j, 0)));
         const float aEh = __double2float_rn(aE);
         const float aEl = __double2float_rn(aE - (double)aEh);
-        float A = 1.0f, D = 1.0f;  // u_{j0} = 1, u_{j0-1} = 0
-        float Ao = 1.0f, Do = 1.0f;
+        // outward: u_{j0} = 1, u_{j0-1} = 0; inward: v_{j1} = 1, v_{j1+1} = 0
+        float A = 1.0f, D = 1.0f;
         int nodes = 0;
-        bool inward = false;
         const TileSeq seq = make_seq(j0, j1, k, kCountTile);
-        for (int t = 0; t < seq.size(); ++t) {
-            const int T0 = seq.tile(t) * kCountTile;
-            __syncthreads();  // the previous tile is consumed
-            for (int x = tid; x < kCountTile; x += kCountThreads) tile[x] = src[T0 + x];
+        const int L = max(seq.n_out, seq.n_in);
+        for (int t = 0; t < L; ++t) {
+            const int To = t < seq.n_out ? seq.tile(t) * kCountTile : -1;
+            const int Ti = t < seq.n_in ? seq.tile(seq.n_out + t) * kCountTile : -1;
+            __syncthreads();  // the previous tiles are consumed
+            for (int x = tid; x < kCountTile; x += kCountThreads) {
+                if (To >= 0) tile_o[x] = src[To + x];
+                if (Ti >= 0) tile_i[x] = src[Ti + x];
+            }
             __syncthreads();
-            if (t < seq.n_out) {
-                run_up_raw(tile, T0, max(j0, T0), min(k - 1, T0 + kCountTile - 1), aEh, aEl, A, D, nodes);
-            } else {
-                if (!inward) {
-                    inward = true;
-                    Ao = A;
-                    Do = D;
-                    A = 1.0f;  // v_{j1} = 1, v_{j1+1} = 0
-                    D = 1.0f;
-                }
-                run_down_raw(tile, T0, min(j1, T0 + kCountTile - 1), max(k + 1, T0), aEh, aEl, A, D, nodes);
+            if (side == 0) {
+                if (To >= 0)
+                    run_up_raw(tile_o, To, max(j0, To), min(k - 1, To + kCountTile - 1), aEh, aEl, A, D, nodes);
+            } else if (Ti >= 0) {
+                run_down_raw(tile_i, Ti, min(j1, Ti + kCountTile - 1), max(k + 1, Ti), aEh, aEl, A, D, nodes);
             }
         }
-        if (!inward) {  // no inward tiles: k == j1
-            Ao = A;
-            Do = D;
-            A = 1.0f;
-            D = 1.0f;
+        if (side == 1) {
+            s_A[e] = A;
+            s_D[e] = D;
+            s_nodes[e] = nodes;
         }
-        // twist pivot sign in FP64: -12 T_k u_k v_k + f_k (D_o v_k + D_i u_k)
-        const double Tk = aE - b.W64[m.off + k];
-        const double fk = 1.0 + Tk;
-        const double uA = (double)Ao, vC = (double)A;
-        const double AC = uA * vC;
-        const double num = -12.0 * Tk * AC + fk * ((double)Do * vC + (double)D * uA);
-        nodes += (num < 0.0) != (AC < 0.0);
-        if (j >= 0) b.counts[(int64_t)p * b.n_trial + j] = nodes;
+        __syncthreads();
+        if (side == 0) {
+            // twist pivot sign in FP64: -12 T_k u_k v_k + f_k (D_o v_k + D_i u_k)
+            const double Tk = aE - b.W64[m.off + k];
+            const double fk = 1.0 + Tk;
+            const double uA = (double)A, vC = (double)s_A[e];
+            const double AC = uA * vC;
+            const double num = -12.0 * Tk * AC + fk * ((double)D * vC + (double)s_D[e] * uA);
+            nodes += s_nodes[e] + ((num < 0.0) != (AC < 0.0));
+            if (j >= 0) b.counts[(int64_t)p * b.n_trial + j] = nodes;
+        }
     }
 }
 
