@@ -50,7 +50,7 @@ struct OrI {
 __global__ void __launch_bounds__(kPrepThreads) prepare_kernel(DevBatch b) {
     __shared__ double shd[32];
     __shared__ int shi[32];
-    const int p = blockIdx.x;
+    const int p = b.order[blockIdx.x];  // longest grids first (the tail is the last CTAs)
     PotMeta m = b.meta[p];
     const double* V = b.V64 + m.off;
     const int N = m.N;
