@@ -52,6 +52,8 @@ class Opts(C.Structure):
         ("stream", C.c_void_p),
         ("tune", C.c_int32),
         ("long_window", C.c_int32),
+        ("wait_polls", C.c_int32),
+        ("max_iter", C.c_int32),
     ]
 
 
@@ -117,6 +119,10 @@ class Stats(C.Structure):
         ("reserved2", C.c_int32),
         ("long_fp32_point_updates", C.c_int64),
         ("long_df_point_updates", C.c_int64),
+        ("ms_zero_psi", C.c_float),
+        ("reserved3", C.c_int32),
+        ("psi_zero_points", C.c_int64),
+        ("psi_window_points", C.c_int64),
     ]
 
 
@@ -134,6 +140,7 @@ EXPORTED = [
     "epscu_adjoint_psi",
     "epscu_tabulate",
     "epscu_cancel",
+    "epscu_cancel_clear",
     "epscu_last_stats",
     "epscu_measure_fma_peaks",
     "epscu_count_levels_static",
@@ -175,6 +182,7 @@ def load(build_if_missing: bool = True):
                                     C.POINTER(Opts)]
     L.epscu_tabulate.argtypes = [C.c_void_p, C.c_int32, _ip, _dp, _lp, _ip, _dp, _dp, C.c_int32, _dp, C.POINTER(Opts)]
     L.epscu_cancel.argtypes = [C.c_void_p]
+    L.epscu_cancel_clear.argtypes = [C.c_void_p]
     L.epscu_last_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
     L.epscu_measure_fma_peaks.argtypes = [C.c_void_p, _dp, _dp]
     L.epscu_count_levels_static.argtypes = [_dp, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_double,
@@ -228,6 +236,8 @@ class Solution:
     psi: np.ndarray | None
     psi_offsets: np.ndarray
     N: np.ndarray
+    rc: int = 0  # status code of the solve (epscu_solve's return value)
+    psi_required: int = 0  # doubles the wavefunctions of this solve need
 
     def levels(self, p: int) -> np.ndarray:
         return self.energy[p, : self.n_out[p]]
@@ -286,6 +296,9 @@ class Context:
     def cancel(self):
         _check(self._lib.epscu_cancel(self._h))
 
+    def cancel_clear(self):
+        _check(self._lib.epscu_cancel_clear(self._h))
+
     def stats(self) -> Stats:
         s = Stats()
         _check(self._lib.epscu_last_stats(self._h, C.byref(s)))
@@ -315,12 +328,18 @@ class Context:
         long_window: int = 0,
         keep_psi: bool = False,
         out: Solution | None = None,
+        wait_polls: int = 0,
+        max_iter: int = 0,
+        check: bool = True,
     ) -> Solution:
         """Solve a batch of host potentials (host buffers through the C ABI).
 
         out: a Solution of this batch's shape whose result arrays are written
         in place (for instance page-locked buffers reused across solves, so
-        the device-to-host copies run at full speed); its psi is not used."""
+        the device-to-host copies run at full speed); its psi is not used.
+        wait_polls / max_iter: epscu_opts bounds (0: the defaults).
+        check=False returns the Solution with the status code in .rc instead
+        of raising on a non-zero code."""
         V, offsets, N = concat(Vs)
         n = int(N.size)
 
@@ -372,9 +391,15 @@ class Context:
             0,
         )
         flags = (WANT_PSI if want_psi else 0) | (KEEP_PSI if keep_psi and not want_psi else 0)
-        o = Opts(int(method), flags, float(tol), None, 1 if tune else 0, int(long_window))
-        _check(self._lib.epscu_solve(self._h, C.byref(b), C.byref(r), C.byref(o)))
-        return Solution(n_total, n_out, energy, nodes, status, err, psi, psi_off, N)
+        o = Opts(int(method), flags, float(tol), None, 1 if tune else 0, int(long_window), int(wait_polls),
+                 int(max_iter))
+        rc = self._lib.epscu_solve(self._h, C.byref(b), C.byref(r), C.byref(o))
+        if check:
+            _check(rc)
+        sol = Solution(n_total, n_out, energy, nodes, status, err, psi, psi_off, N)
+        sol.rc = int(rc)
+        sol.psi_required = int(r.psi_required)
+        return sol
 
     def adjoint(self, dL_dE: np.ndarray, total_points: int, recompute: bool = False,
                 out: np.ndarray | None = None) -> np.ndarray:

@@ -84,6 +84,8 @@ struct Header {
     int32_t pad_hdr;
     unsigned long long long32_updates;      // refine_long (long list): FP32 pass point-updates
     unsigned long long longdf_updates;      //   and double-float pass point-updates
+    unsigned long long psi_zero_points;     // psi points zeroed by zero_psi (outside the windows)
+    unsigned long long psi_window_points;   // window points scale_psi converted
 };
 
 // queue ids of the per-level kernels

@@ -60,7 +60,7 @@ struct DevBuf {
     size_t cap = 0;
 };
 
-constexpr int kStageEvents = 10;  // 0-6 stages, 6-7 autotune, 8-9 around refine_long
+constexpr int kStageEvents = 12;  // 0-6 stages, 6-7 autotune, 8-9 around refine_long, 10-11 around zero_psi
 
 }  // namespace
 
@@ -269,7 +269,14 @@ epscu_status epscu_set_arena_block(epscu_ctx* ctx, int64_t bytes) {
 
 epscu_status epscu_cancel(epscu_ctx* ctx) {
     if (!ctx) return fail(EPSCU_ERR_INVALID, "ctx is NULL");
-    *ctx->cancel_host = 1;  // no lock: the solve holds it
+    // no lock (a running solve holds it); the kernels read the mapped flag
+    __atomic_store_n(const_cast<int32_t*>(ctx->cancel_host), 1, __ATOMIC_RELEASE);
+    return EPSCU_OK;
+}
+
+epscu_status epscu_cancel_clear(epscu_ctx* ctx) {
+    if (!ctx) return fail(EPSCU_ERR_INVALID, "ctx is NULL");
+    __atomic_store_n(const_cast<int32_t*>(ctx->cancel_host), 0, __ATOMIC_RELEASE);
     return EPSCU_OK;
 }
 
@@ -351,7 +358,9 @@ void enqueue_pipeline(epscu_ctx* ctx, const DevBatch& b, int method, bool want_p
             rec(3);
             launch_newton_df(b, ctx->sm_count, s);
             launch_fallback_long(b, ctx->sm_count, s);
+            rec(10);
             if (want_psi) launch_zero_psi(b, ctx->sm_count, s);
+            rec(11);
             launch_norm_df(b, ctx->sm_count, s);
             launch_norm_long(b, ctx->sm_count, s);
             launch_twist_long(b, ctx->sm_count, s);
@@ -509,6 +518,8 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     if (!b.twist_scratch || !b.twist_list) return fail(EPSCU_ERR_NOMEM, "device arena (twist search)");
     b.tol = opts.tol;
     b.long_window = opts.long_window > 0 ? opts.long_window : 0;  // 0: chosen from the level count
+    b.wait_polls = opts.wait_polls;  // 0: the default bound; < 0: the failure self-test
+    b.max_iter = opts.max_iter > 0 ? opts.max_iter : 0;            // 0: the default caps
     b.psi = nullptr;
     b.psi_capacity = 0;
     if (want_psi) {
@@ -541,7 +552,8 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     auto* hh = (Header*)ctx->host("hdr", sizeof(Header), &ce);
     if (!hh) return fail(EPSCU_ERR_NOMEM, "pinned staging (hdr)");
     std::memset(hh, 0, sizeof(Header));
-    *ctx->cancel_host = 0;
+    // (the cancel flag is not cleared here: a request made before the solve
+    // starts stops this solve, which consumes it below)
 
     // ---- launch shape of the FP32 scan (autotuned per batch shape)
     ScanShape shape{256, 2048, 3, 0};
@@ -705,7 +717,10 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
         }
         st.ms_write = el(4, 5);
         st.ms_total = el(0, 6);
-        if (method == EPSCU_METHOD_FAST_FP32C) st.ms_refine_long = el(8, 9);
+        if (method == EPSCU_METHOD_FAST_FP32C) {
+            st.ms_refine_long = el(8, 9);
+            st.ms_zero_psi = el(10, 11);
+        }
     } else {
         cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[6]);
         st.ms_total = ms;
@@ -748,6 +763,8 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
         st.refine_max_iters = hh->refine_max_iters;
         st.long_fp32_point_updates = (int64_t)hh->long32_updates;
         st.long_df_point_updates = (int64_t)hh->longdf_updates;
+        st.psi_zero_points = (int64_t)hh->psi_zero_points;
+        st.psi_window_points = (int64_t)hh->psi_window_points;
     }
     ctx->stats = st;
 
@@ -760,10 +777,14 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     ctx->last_total_points = total_points;
     ctx->last_psi_total = psi_total;
 
+    // a cancel request is consumed by the solve it reached
+    const bool cancelled = __atomic_exchange_n(const_cast<int32_t*>(ctx->cancel_host), 0, __ATOMIC_ACQ_REL) != 0;
     if (hh->error == EPSCU_ERR_CAPACITY || (want_psi && psi_total > res->psi_capacity))
         return fail(EPSCU_ERR_CAPACITY, "psi buffer too small: " + std::to_string(psi_total) + " doubles required");
+    if (hh->error == EPSCU_ERR_TIMEOUT)
+        return fail(EPSCU_ERR_TIMEOUT, "a bounded wait of the TMA scan ran out (results incomplete)");
     if (hh->error) return fail(hh->error, "device-side error " + std::to_string(hh->error));
-    if (*ctx->cancel_host) return fail(EPSCU_ERR_CANCELLED, "solve cancelled");
+    if (cancelled) return fail(EPSCU_ERR_CANCELLED, "solve cancelled");
     return EPSCU_OK;
 }
 

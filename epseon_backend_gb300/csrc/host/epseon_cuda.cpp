@@ -333,8 +333,7 @@ std::shared_ptr<ComputeDeviceInterface> ComputeContext::getDeviceInterface(uint3
 template <typename FP>
 TaskHandle<FP>::~TaskHandle() {
     if (worker.joinable()) {
-        worker.request_stop();
-        if (device && device->context()) epscu_cancel(device->context());
+        cancel();
         worker.join();
     }
 }
@@ -374,14 +373,22 @@ void TaskHandle<FP>::run(std::stop_token st, TaskHandle* self) {
             self->setMessage("failed");
         }
     }
+    {
+        std::lock_guard<std::mutex> g(self->run_mu);
+        self->finished = true;
+    }
     self->done.store(true, std::memory_order_release);
 }
 
 template <typename FP>
 bool TaskHandle<FP>::cancel() {
-    if (!isRunning()) return false;
+    if (!isStarted()) return false;
+    std::lock_guard<std::mutex> g(run_mu);
+    if (finished) return false;
     const bool r = worker.request_stop();
-    if (device && device->context()) epscu_cancel(device->context());
+    // the device solve in flight polls the context's flag; between solves the
+    // worker sees the stop request before it starts the next one
+    if (in_solve && device && device->context()) epscu_cancel(device->context());
     return r;
 }
 
@@ -458,7 +465,24 @@ void TaskHandle<FP>::execute(std::stop_token st) {
         o.flags = psi.empty() ? 0 : EPSCU_WANT_PSI;
         o.tol = 1e-12;
         setMessage("solving potentials " + std::to_string(first) + ".." + std::to_string(first + count));
-        const epscu_status s = epscu_solve(ctx, &b, &r, &o);
+        epscu_status s;
+        {
+            std::lock_guard<std::mutex> solve_guard(device->solveMutex());
+            {
+                std::lock_guard<std::mutex> g(run_mu);
+                if (st.stop_requested()) {
+                    setMessage("cancelled");
+                    return;
+                }
+                in_solve = true;
+            }
+            s = epscu_solve(ctx, &b, &r, &o);
+            std::lock_guard<std::mutex> g(run_mu);
+            in_solve = false;
+            // a request that reached the context after the solve consumed its
+            // flag would stop the next solve of another task: withdraw it
+            if (st.stop_requested()) epscu_cancel_clear(ctx);
+        }
         if (s == EPSCU_ERR_CANCELLED || st.stop_requested()) {
             setMessage("cancelled");
             return;

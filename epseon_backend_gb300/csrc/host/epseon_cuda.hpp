@@ -257,6 +257,12 @@ class TaskHandle : public std::enable_shared_from_this<TaskHandle<FP>> {
     std::string message = "created";
     TaskResults res;
     std::exception_ptr error;
+    // cancel() and the worker agree under run_mu: the context's flag is set
+    // only while this task's solve runs (in_solve), and a request that came
+    // after that solve had already finished is withdrawn by the worker
+    std::mutex run_mu;
+    bool in_solve = false;
+    bool finished = false;
     std::jthread worker;
 };
 
@@ -304,10 +310,15 @@ class ComputeDeviceInterface : public std::enable_shared_from_this<ComputeDevice
     }
     epscu_ctx* context() const { return ctx; }
     int32_t ordinal() const { return ord; }
+    // held by a task for the whole of each of its solves: tasks on one device
+    // interface take the context in turn, so a task's cancel request reaches
+    // the context only while that task's own solve holds it
+    std::mutex& solveMutex() { return solve_mu; }
 
   private:
     int32_t ord;
     epscu_ctx* ctx = nullptr;
+    std::mutex solve_mu;
 };
 
 class ComputeContext : public std::enable_shared_from_this<ComputeContext> {

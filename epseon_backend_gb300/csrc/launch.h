@@ -44,8 +44,16 @@ struct DevBatch {
     int32_t min_level, max_level;
     int32_t max_N;             // longest grid of the batch
     int32_t long_window;       // window length above which a level takes the CTA passes
+    int32_t wait_polls;        // polls of a bounded wait on a staged scan tile (0: kWaitPolls)
+    int32_t max_iter;          // cap on FP32 refinement passes (0: 48; fallback passes: twice it)
     double tol;
 };
+
+constexpr int kWaitPolls = 1 << 22;       // default bound of the TMA scan's mbarrier waits
+constexpr int kRefineMaxIter = 48;        // default cap on a level's FP32 refinement passes
+__device__ __forceinline__ int refine_cap(const DevBatch& b) { return b.max_iter > 0 ? b.max_iter : kRefineMaxIter; }
+// double-float fallback passes (bisection from the widened scan bracket)
+__device__ __forceinline__ int fallback_cap(const DevBatch& b) { return 2 * refine_cap(b); }
 
 // Warp-level work queue of the per-level kernels: units of up to 32
 // consecutive level slots of one potential, longest grids first.  Lane 0

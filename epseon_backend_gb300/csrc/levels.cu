@@ -339,7 +339,7 @@ __global__ void __launch_bounds__(kLevelThreads, 4) refine32_kernel(DevBatch b) 
         // recomputes the sum there (a stale sum is off by (psi_k_old/psi_k)^2
         // and slows Newton to a crawl)
         bool final_pass = false;
-        for (; it < 48 || final_pass; ++it) {
+        for (const int cap = refine_cap(b); it < cap || final_pass; ++it) {
             const Pass32 r = cooley32(m, Wf, W64, E, k, w.j0, w.j1);
             sum = r.sum;
             k_sum = k;

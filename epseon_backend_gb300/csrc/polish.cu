@@ -373,33 +373,56 @@ __global__ void __launch_bounds__(kThreads, 4) write_df_kernel(DevBatch b) {
     }
 }
 
-// Zeros over the batch's psi rows (the first psi_total doubles), run beside
-// the compute-bound refinement kernels so that the write-back only touches
-// the windows (~a fifth of the rows on the mixed batch).
+// Zeros of the psi rows outside each level's window (the whole row of a
+// level that has no result yet), run beside the compute-bound refinement
+// kernels.  The windows are final once the window kernel has run; their
+// points are written by the norm passes and scale_psi, so every point of a
+// row is written once by one of the two (the window is ~a fifth of the row
+// on the mixed batch).  One warp per level, coalesced stores.
 __global__ void __launch_bounds__(256) zero_psi_kernel(DevBatch b) {
     if (!b.psi || b.hdr->error) return;
-    const long long n = min(b.hdr->psi_total, (long long)b.psi_capacity);
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        b.psi[i] = 0.0;
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int n_warps = (gridDim.x * blockDim.x) >> 5;
+    const int total = b.hdr->total_levels;
+    unsigned long long zeroed = 0;
+    for (int slot = warp; slot < total; slot += n_warps) {
+        const LevelWork w = b.levels[slot];
+        const PotMeta m = b.meta[w.p];
+        const int N = m.N;
+        double* row = b.psi + m.psi_off + (int64_t)(w.v - b.min_level) * N;
+        const bool none = no_result(w);
+        const int a = none ? N : w.j0, c = none ? N : w.j1 + 1;
+        for (int i = lane; i < a; i += 32) row[i] = 0.0;
+        for (int i = c + lane; i < N; i += 32) row[i] = 0.0;
+        zeroed += (unsigned long long)(a + (N - c));
+    }
+    if (lane == 0 && zeroed) atomicAdd(&b.hdr->psi_zero_points, zeroed);
 }
 
 // The write-back of the fused norm/write: each row holds the unnormalised
 // psi-hat of the level's final norm pass (norm_df, norm_long or twist_long)
 // on [j0, k) and (k, j1] as scaled float pairs; scale it by the
 // side constants (norm_k 2^-ex) and set psi_k = ck.  The rest of the row was
-// zeroed by zero_psi.  One warp per level, coalesced: HBM-bound (8 B read +
-// 8 B written per window point).
+// zeroed by zero_psi; the window of a level left without a result is zeroed
+// here.  One warp per level, coalesced: HBM-bound (8 B read + 8 B written per
+// window point).
 __global__ void __launch_bounds__(256) scale_psi_kernel(DevBatch b) {
     if (!b.psi || b.hdr->error) return;
     const int lane = threadIdx.x & 31;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int n_warps = (gridDim.x * blockDim.x) >> 5;
     const int total = b.hdr->total_levels;
+    unsigned long long converted = 0;
     for (int slot = warp; slot < total; slot += n_warps) {
         const LevelWork w = b.levels[slot];
         const PotMeta m = b.meta[w.p];
         double* row = b.psi + m.psi_off + (int64_t)(w.v - b.min_level) * m.N;
-        if (no_result(w)) continue;
+        if (no_result(w)) {
+            for (int i = w.j0 + lane; i <= w.j1; i += 32) row[i] = 0.0;
+            continue;
+        }
+        converted += (unsigned long long)(w.j1 - w.j0 + 1);
         // the side constants norm_k 2^-ex as m 2^e, m in [0.5, 1) a
         // double-float: per point the pair times m in double-float and the
         // double assembled with integer operations, scaled by 2^(64 r + e)
@@ -429,6 +452,7 @@ __global__ void __launch_bounds__(256) scale_psi_kernel(DevBatch b) {
         }
         for (; i <= w.j1; i += 32) row[i] = convert(i, pair[i]);
     }
+    if (lane == 0 && converted) atomicAdd(&b.hdr->psi_window_points, converted);
 }
 
 }  // namespace

@@ -189,16 +189,25 @@ __global__ void __launch_bounds__(kPrepThreads) prepare_kernel(DevBatch b) {
 
 // Level counts per potential, exclusive prefix sums (level slots and psi
 // offsets) and the total level count.  One CTA.
+// A solve cancelled before this point, or whose scan gave up on a bounded wait
+// (the error word is set), may have skipped scan work: its counts are
+// incomplete and it gets no levels.  The cancel flag only goes from 0 to 1
+// while a solve runs, so a scan that saw it is always followed by a set-up
+// that does.
 __global__ void __launch_bounds__(1024) level_setup_kernel(DevBatch b) {
     __shared__ int32_t s_lv[1024];
     __shared__ long long s_ps[1024];
     __shared__ int32_t carry_lv;
     __shared__ long long carry_ps;
+    __shared__ int s_cancelled, s_failed;
     if (threadIdx.x == 0) {
         carry_lv = 0;
         carry_ps = 0;
+        s_cancelled = b.cancel && *b.cancel;
+        s_failed = b.hdr->error != 0;
     }
     __syncthreads();
+    const bool cancelled = s_cancelled != 0, failed = s_failed != 0;
     for (int base = 0; base < b.n; base += blockDim.x) {
         const int p = base + threadIdx.x;
         int32_t n_out = 0;
@@ -206,7 +215,8 @@ __global__ void __launch_bounds__(1024) level_setup_kernel(DevBatch b) {
         if (p < b.n) {
             PotMeta& m = b.meta[p];
             int32_t n_total = 0;
-            if (!(m.status & EPSCU_STATUS_BAD)) n_total = b.counts[(int64_t)p * b.n_trial + b.n_trial - 1];
+            if (cancelled) m.status |= EPSCU_STATUS_CANCELLED;
+            else if (!failed && !(m.status & EPSCU_STATUS_BAD)) n_total = b.counts[(int64_t)p * b.n_trial + b.n_trial - 1];
             int32_t last = b.max_level < 0 ? n_total - 1 : min(b.max_level, n_total - 1);
             n_out = last - b.min_level + 1;
             n_out = max(0, min(n_out, b.level_capacity));

@@ -71,9 +71,31 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 
+// non-blocking test of a phase
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
 // Bounded wait on a phase of an mbarrier; false when the limit ran out.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-    for (int it = 0; it < (1 << 22); ++it)
+// polls == 0: up to kWaitPolls try_waits, each of which may suspend the
+// thread for a hardware-defined time until the phase completes; polls > 0
+// (epscu_opts.wait_polls): that many non-blocking tests, a bound measured in
+// instructions rather than in copy latency.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int polls = 0) {
+    if (polls > 0) {
+        for (int it = 0; it < polls; ++it)
+            if (mbar_test_wait(bar, parity)) return true;
+        return false;
+    }
+    for (int it = 0; it < kWaitPolls; ++it)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -226,17 +248,20 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
     float2* buf = reinterpret_cast<float2*>(smem_raw);               // STAGES TMA tiles of (w.x, w.y)
     float* conv = reinterpret_cast<float*>(buf + (size_t)STAGES * TILE);  // the converted tile
     __shared__ __align__(8) uint64_t full[STAGES];
+    __shared__ __align__(8) uint64_t never;  // the failure self-test's barrier: nothing arrives
     __shared__ int s_item;
     __shared__ int s_abort;
 
     const int tid = threadIdx.x;
     if (tid == 0) {
         for (int s = 0; s < STAGES; ++s) mbar_init(&full[s], 1);
+        mbar_init(&never, 1);
         fence_barrier_init();
         s_abort = 0;
     }
     __syncthreads();
 
+    const int wait_polls = b.wait_polls > 0 ? b.wait_polls : 0;
     uint32_t g_tile = 0;   // tiles consumed by this CTA so far (phase bookkeeping)
     uint32_t g_issue = 0;  // tiles issued by this CTA so far (thread 0)
     for (;;) {
@@ -301,6 +326,16 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
             }
         }
 
+        if (b.wait_polls < 0) {
+            // self-test of the failure path (epscu_opts.wait_polls < 0): a wait
+            // that runs out, on a barrier no copy completes, taken exactly as
+            // a lost copy is (abort, drain the copies in flight, error word)
+            if (!mbar_wait_bounded(&never, 0, -b.wait_polls)) {
+                atomicExch(&s_abort, 1);
+                atomicCAS(&b.hdr->error, 0, EPSCU_ERR_TIMEOUT);
+            }
+        }
+
         const double E = trial_energy(m, j);
         const double aE = __dmul_rn(m.a, E);
         // the item's reference energy (middle of its block) and this thread's
@@ -316,7 +351,7 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
         for (int t = 0; t < L; ++t) {
             const int st = (g_tile + t) % STAGES;
             const uint32_t par = ((g_tile + t) / STAGES) & 1u;
-            const bool landed = mbar_wait_bounded(&full[st], par);
+            const bool landed = mbar_wait_bounded(&full[st], par, wait_polls);
             if (!landed) {
                 atomicExch(&s_abort, 1);
                 atomicCAS(&b.hdr->error, 0, EPSCU_ERR_TIMEOUT);
@@ -377,7 +412,9 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
     }
     __syncthreads();
     if (s_abort && tid == 0) {
-        // drain: wait (bounded) for the copies issued but never consumed
+        // drain: wait (bounded, always with the default limit so that no copy
+        // is still landing in this CTA's shared memory when it exits) for the
+        // copies issued but never consumed
         for (uint32_t q = g_tile; q < g_issue; ++q) (void)mbar_wait_bounded(&full[q % STAGES], (q / STAGES) & 1u);
     }
 }

@@ -20,6 +20,10 @@
 //    header is cleared on the device at the start of each call.  Calls that
 //    overlap on the GPU (different streams, or several host threads) race on
 //    the array and must be serialised by the caller.
+//  * The call returns before the GPU has run it, so a failure found on the
+//    device (bad input flagged by the prepare kernel, a bounded wait of the
+//    scan that ran out) is reported in the output: a last one-CTA kernel
+//    then sets every count to EPSCU_STATIC_FAILED (-1).
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -61,6 +65,16 @@ __global__ void static_init_kernel(StaticScanScratch* s, double r_min, double r_
     Header h{};
     s->hdr = h;  // the scan's work queue starts at zero on every call
     s->order[0] = 0;
+}
+
+// Runs after the scan on the same stream: a device-side failure of the call
+// (the scan's error word, or a potential the prepare kernel rejected) turns
+// every count into EPSCU_STATIC_FAILED, so the caller can tell a failed call
+// from a potential with no bound levels.
+__global__ void static_finish_kernel(const StaticScanScratch* s, int32_t n_trial, int32_t* counts) {
+    const bool failed = s->hdr.error != 0 || (s->meta.status & EPSCU_STATUS_BAD) != 0;
+    if (!failed) return;
+    for (int j = threadIdx.x; j < n_trial; j += blockDim.x) counts[j] = EPSCU_STATIC_FAILED;
 }
 
 constexpr int kMaxDevices = 64;
@@ -129,6 +143,7 @@ extern "C" epscu_status epscu_count_levels_static(const double* V, int32_t N, do
     launch_prepare(b, s);
     const ScanShape shape{256, 2048, 3, 0};
     launch_scan32(b, shape, sm_count, s);
+    static_finish_kernel<<<1, 1024, 0, s>>>(S, n_trial, counts);
     e = cudaGetLastError();
     if (e != cudaSuccess) return static_fail(EPSCU_ERR_CUDA, cudaGetErrorString(e));
     return EPSCU_OK;

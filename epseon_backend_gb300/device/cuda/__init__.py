@@ -23,3 +23,19 @@ from ._libepseon_cuda import (  # noqa: F401
     TaskHandleFloat32,
     TaskHandleFloat64,
 )
+
+__all__ = [
+    "ComputeDeviceInterface",
+    "EpseonComputeContext",
+    "LennardJonesPotentialConfig",
+    "MemoryHeap",
+    "MemoryType",
+    "MorsePotentialConfig",
+    "PhysicalDeviceInfo",
+    "PhysicalDeviceProperties",
+    "PhysicalDeviceSparseProperties",
+    "TaskConfiguratorFloat32",
+    "TaskConfiguratorFloat64",
+    "TaskHandleFloat32",
+    "TaskHandleFloat64",
+]

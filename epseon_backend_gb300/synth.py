@@ -177,6 +177,23 @@ def tabulate(b: PotentialBatch, i: int) -> np.ndarray:
     return spline_eval(r, b.r_min[i], hk, yk, M)
 
 
+def tabulate_params(kind: int, P: np.ndarray, N: int, r_min: float, r_max: float,
+                    n_knots: int = N_KNOTS) -> np.ndarray:
+    """Host tabulation of one [12] parameter row in the layout epscu_tabulate
+    takes: Morse (De, a, re) or LJ (eps, sigma) at P[0:3], bumps (amp, width,
+    centre) x 3 at P[3:12] (Morse + bumps through the natural spline)."""
+    P = np.asarray(P, np.float64)
+    r = r_min + np.arange(int(N)) * ((r_max - r_min) / (int(N) - 1))
+    if int(kind) == KIND_MORSE:
+        return morse(r, P[0], P[1], P[2])
+    if int(kind) == KIND_LJ:
+        return lennard_jones_shifted(r, P[0], P[1])
+    rk = np.linspace(r_min, r_max, n_knots)
+    yk = morse(rk, P[0], P[1], P[2]) + bumps_at(rk, P[3:12].reshape(3, 3))
+    hk = (r_max - r_min) / (n_knots - 1)
+    return spline_eval(r, r_min, hk, yk, natural_spline_second_derivs(yk, hk))
+
+
 def _loguniform(rng, lo, hi, n):
     return np.exp(rng.uniform(np.log(lo), np.log(hi), n))
 

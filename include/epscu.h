@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define EPSCU_ABI_VERSION 1
+#define EPSCU_ABI_VERSION 2
 
 typedef int32_t epscu_status;
 enum {
@@ -104,6 +104,17 @@ typedef struct epscu_opts {
     int32_t long_window; /* fast method: levels whose window exceeds this many points run
                             their passes one CTA per level (0: chosen from the number of
                             levels, 1024 - 8192) */
+    int32_t wait_polls;  /* fast method: bound of each wait of the TMA scan on a staged
+                            tile, in non-blocking polls; when it runs out the solve gives up
+                            with EPSCU_ERR_TIMEOUT and reports no levels.  0: the default,
+                            4194304 polls that may each suspend until the copy lands.  The
+                            copies already in flight are still drained with the default
+                            bound, so the context stays usable.  < 0: self-test of that
+                            failure path: every scan item first waits -wait_polls polls on
+                            a barrier that no copy completes, and gives up as above. */
+    int32_t max_iter;    /* fast method: cap on the FP32 refinement passes of a level and
+                            on its double-float fallback passes (0: 48 and 96); a level
+                            that reaches it carries EPSCU_LEVEL_MAXITER */
 } epscu_opts;
 
 /* Caller-owned outputs.  Level slot s of potential p is p*level_capacity + s
@@ -200,10 +211,20 @@ epscu_status epscu_tabulate(epscu_ctx* ctx, int32_t n, const int32_t* kind, cons
                             const int64_t* offsets, const int32_t* N, const double* r_min,
                             const double* r_max, int32_t n_knots, double* V, const epscu_opts* opts);
 
-/* Cooperative cancellation of the solve running on ctx (TaskHandle::cancel,
- * cpp/gpu/include/epseon/gpu/task_handle.hpp:136-144).  The persistent
- * kernels poll a host-mapped flag between work items. */
+/* Cooperative cancellation (TaskHandle::cancel,
+ * cpp/gpu/include/epseon/gpu/task_handle.hpp:136-144).  Sets a host-mapped
+ * flag that the persistent kernels poll between work items.  The request
+ * stops the solve running on ctx or, when none is running, the next solve
+ * to start; the solve it stops consumes it (returns EPSCU_ERR_CANCELLED and
+ * clears the flag).  A solve stopped before its level set-up reports no
+ * levels; levels set up before the request carry EPSCU_LEVEL_CANCELLED. */
 epscu_status epscu_cancel(epscu_ctx* ctx);
+
+/* Withdraws a cancel request that no solve has consumed (the reference's
+ * request_stop is per task, task_handle.hpp:136-144; a context shared by
+ * several tasks needs this so that a request which arrived after its task's
+ * last solve does not stop another task's solve). */
+epscu_status epscu_cancel_clear(epscu_ctx* ctx);
 
 /* Timing of the last solve: per-stage milliseconds (CUDA events on the solve
  * stream) and the counters the roofline uses.  Stages: prepare (set-up and,
@@ -236,6 +257,14 @@ typedef struct epscu_stats {
     int32_t reserved2;
     int64_t long_fp32_point_updates;
     int64_t long_df_point_updates;
+    /* the psi write-back of the fast method: zero_psi writes zeros outside the
+       level windows (its time with EPSCU_STAGE_TIMING only; ms_write is the
+       time of scale_psi, which reads the window's stored pairs and writes the
+       normalised doubles) */
+    float ms_zero_psi;
+    int32_t reserved3;
+    int64_t psi_zero_points;   /* points zero_psi wrote (8 B each) */
+    int64_t psi_window_points; /* window points scale_psi converted (8 B read + 8 B written each) */
 } epscu_stats;
 epscu_status epscu_last_stats(epscu_ctx* ctx, epscu_stats* stats);
 
@@ -254,10 +283,19 @@ epscu_status epscu_measure_fma_peaks(epscu_ctx* ctx, double* fp32_tflops, double
  *            E_j = min V + (j+1) (e_cap - min V) / n_trial
  *   stream : cudaStream_t the work is queued on (NULL: legacy default stream);
  *            the call returns without synchronising.
+ * The counts come from the fast method's FP32 difference-form scan: reliable
+ * to about 1e-9 Hartree, so a trial energy within ~1e-9 Eh of a level may be
+ * counted on either side of it (epscu_solve's plain FP64 method gives exact
+ * counts).  Failures found on the device cannot change the return code of an
+ * asynchronous call: the call then sets every one of the n_trial counts to
+ * -1 (EPSCU_STATIC_FAILED).  That happens for a non-finite potential, a grid
+ * with fewer than three points inside its cut-offs, e_cap <= min V, and a
+ * bounded wait of the scan that ran out.
  * Grids longer than 65536 points return EPSCU_ERR_CAPACITY.  The first call
  * on each device looks up the scratch's device address (make it before any
  * stream capture).  All calls share the scratch: calls that overlap on the GPU
  * race and must be serialised by the caller. */
+#define EPSCU_STATIC_FAILED (-1)
 epscu_status epscu_count_levels_static(const double* V, int32_t N, double r_min, double r_max, double mu,
                                        double e_cap, int32_t n_trial, int32_t* counts, void* stream);
 

@@ -36,7 +36,7 @@ def test_header_declarations_are_all_exported(lib):
 
 def test_abi_version_and_errors_without_device(lib):
     L = capi.load()
-    assert L.epscu_abi_version() == 1
+    assert L.epscu_abi_version() == 2
     # invalid arguments are rejected before any CUDA call
     assert L.epscu_create(0, None) == capi.ERR_INVALID
     assert b"NULL" in L.epscu_last_error()
@@ -75,3 +75,19 @@ def test_context_without_device_raises():
         pytest.skip("a device is present")
     with pytest.raises(RuntimeError):
         m.EpseonComputeContext.create()
+
+
+def test_reference_import_path():
+    """The reference's package path for devices (epseon_backend.device.<name>)
+    reaches the GB300 device and its extension module unchanged."""
+    _build.build_pymodule()
+    import importlib
+
+    m = importlib.import_module("epseon_backend.device.cuda")
+    ext = importlib.import_module("epseon_backend.device.cuda._libepseon_cuda")
+    import epseon_backend_gb300.device.cuda as own
+
+    assert m.EpseonComputeContext is own.EpseonComputeContext
+    assert ext.TaskConfiguratorFloat32 is own.TaskConfiguratorFloat32
+    for name in own.__all__:
+        assert getattr(m, name) is getattr(own, name)

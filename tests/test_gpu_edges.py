@@ -15,7 +15,7 @@ from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
-E_TOL = {capi.METHOD_PLAIN_FP64: 1e-10, capi.METHOD_FAST_FP32C: 1e-9}
+E_TOL = {capi.METHOD_PLAIN_FP64: 1e-10, capi.METHOD_FAST_FP32C: 1e-10}
 METHODS = [capi.METHOD_PLAIN_FP64, capi.METHOD_FAST_FP32C]
 
 

@@ -188,3 +188,99 @@ def test_tabulated_and_file_potentials(tmp_path):
         outs.append(h.get_results()["energies"][0])
     assert np.allclose(outs[0], outs[1], atol=1e-6)
     assert outs[0].size == 5
+
+
+HARTREE_CM, BOHR_A, DALTON_ME = 219474.6313632, 0.529177210903, 1822.888486209
+
+
+def test_nonuniform_file_matches_oracle(tmp_path):
+    """A two-column (r [angstrom], V [cm^-1]) file on a non-uniform grid takes
+    the loader's resampling branch: a natural cubic spline through the file's
+    points, evaluated on as many uniform points over [r_first, r_last]
+    (potential_source.hpp:44-100 is the reference's stub of this loader).
+    Both precisions against the oracle on the same resampled curve (scipy's
+    natural spline); energies within 1e-10 Hartree, nodes exact."""
+    scipy_interp = pytest.importorskip("scipy.interpolate")
+    from oracle import oracle as O
+
+    t = np.linspace(0.0, 1.0, 4000)
+    r = 2.0 + 10.0 * t ** 1.4  # denser near the inner wall
+    De, a, re = 5000.0, 1.2, 3.0
+    V = De * (1 - np.exp(-a * (r - re))) ** 2 + 0.15 * De * np.exp(-((r - 4.2) ** 2) / (2 * 0.3 ** 2))
+    f = tmp_path / "nonuniform.dat"
+    with open(f, "w") as fh:
+        fh.write("# r[A]\tV[cm-1]\n")
+        for x, y in zip(r, V):
+            fh.write(f"{x!r}\t{y!r}\n")
+    xs = r[0] + (r[-1] - r[0]) / (r.size - 1) * np.arange(r.size)
+    xs[-1] = r[-1]
+    Vu = scipy_interp.CubicSpline(r, V, bc_type="natural")(xs)
+    dist = 0.1
+    mu = 87.62 / 2 * DALTON_ME
+    e_cap = (Vu[-1] - dist) / HARTREE_CM
+    ref = O.solve_batch([Vu / HARTREE_CM], r[0] / BOHR_A, r[-1] / BOHR_A, mu, e_cap, 4096)[0]
+    assert ref.n_total > 20
+    iface = _interface()
+    for precision in ("float64", "float32"):
+        cfg = iface.get_task_configurator(precision).set_hardware_config(
+            potential_buffer_size=4000, group_size=1, allocation_block_size=1 << 24)
+        cfg.set_potential_files([str(f)])
+        cfg.set_vibwa_algorithm(87.62, 87.62, 0.5, dist, 0, ref.n_total + 10)
+        h = iface.submit_task(cfg)
+        h.wait()
+        res = h.get_results()
+        E = res["energies"][0] / HARTREE_CM
+        assert res["n_total"][0] == ref.n_total and E.size == ref.n_total
+        assert np.array_equal(res["nodes"][0], np.arange(E.size))
+        assert np.max(np.abs(E - ref.energy_polished)) < 1e-10, precision
+
+
+def _six_morse(m, point_count=6000):
+    rng = np.random.default_rng(4)
+    return [m.MorsePotentialConfig(dissociation_energy=float(rng.uniform(3000, 6000)),
+                                   equilibrium_bond_distance=float(rng.uniform(2.5, 4.0)),
+                                   well_width=float(rng.uniform(0.8, 1.5)), min_r=1.0, max_r=20.0,
+                                   point_count=point_count) for _ in range(6)]
+
+
+@pytest.mark.parametrize("precision", ["float64", "float32"])
+def test_group_size_splits_reproduce_unsplit_batch(precision):
+    """HardwareConfig.group_size (hardware_config.hpp:16-18) is the number of
+    potentials per device batch.  Splitting a batch into groups of 1 and 4
+    reproduces the unsplit batch: bit for bit with the plain FP64 method (its
+    arithmetic is per potential), within 1e-10 Hartree with the fast method
+    (the long-window threshold follows the batch's level count, so a split
+    may route a level through the other pass of the same precision)."""
+    m = _m()
+    iface = _interface()
+    out = {}
+    for group in (6, 4, 1):
+        cfg = iface.get_task_configurator(precision).set_hardware_config(
+            potential_buffer_size=6000, group_size=group, allocation_block_size=1 << 24)
+        cfg.set_morse_potential(_six_morse(m)).set_vibwa_algorithm(87.62, 87.62, 0.5, 0.1, 0, 80)
+        h = iface.submit_task(cfg)
+        h.wait()
+        out[group] = h.get_results()
+    base = out[6]
+    for group in (4, 1):
+        r = out[group]
+        assert list(r["n_total"]) == list(base["n_total"])
+        for a, b, na, nb in zip(r["energies"], base["energies"], r["nodes"], base["nodes"]):
+            assert np.array_equal(na, nb)
+            if precision == "float64":
+                assert np.array_equal(a, b)
+            else:
+                assert np.max(np.abs(a - b)) < 1e-10 * HARTREE_CM
+
+
+def test_potential_buffer_size_rejects_longer_grids():
+    """HardwareConfig.potential_buffer_size is the longest grid a task
+    accepts: a longer one fails the task with a clear message."""
+    iface = _interface()
+    cfg = _configure(iface.get_task_configurator("float64"))
+    cfg.set_hardware_config(potential_buffer_size=1000, group_size=2, allocation_block_size=1 << 24)
+    h = iface.submit_task(cfg)
+    h.wait()
+    assert h.get_status_message().startswith("failed")
+    with pytest.raises(RuntimeError, match="exceeds potential_buffer_size"):
+        h.get_results()
