@@ -857,7 +857,7 @@ __global__ void __launch_bounds__(kLongThreads) refine_long_kernel(DevBatch b, i
         if (!fallback) {
             // ---- stage 1: FP32
             bool moved_last = false, ok32 = false;
-            for (int it = 0; it < 48; ++it) {
+            for (int it = 0, cap = refine_cap(b); it < cap; ++it) {
                 const PassDF r = long_pass32(m, w, Wf, W, E, k, sh32);
                 ++n_pass32;
                 sum = r.sum;
@@ -915,7 +915,7 @@ __global__ void __launch_bounds__(kLongThreads) refine_long_kernel(DevBatch b, i
             hi = fmin(m.e_cap, w.hi0 + m.delta);
             if (!(E > lo && E < hi)) E = 0.5 * (lo + hi);
             bool moved_last = false;
-            for (int it = 0; it < 96; ++it) {
+            for (int it = 0, cap = fallback_cap(b); it < cap; ++it) {
                 const PassDF r = long_pass<1>(m, w, Wf, W, E, k, 1.0, sh);
                 ++n_pass;
                 sum = r.sum;
