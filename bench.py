@@ -249,6 +249,9 @@ def main():
     ap.add_argument("--long-window", type=int, default=0,
                     help="window length above which a level runs one CTA per level (0: the library's default, "
                          "chosen from the level count)")
+    ap.add_argument("--mid-window", type=int, default=0,
+                    help="window length above which a level runs its double-float passes one warp per level "
+                         "(0: the library's default, < 0: no warp-per-level tier)")
     ap.add_argument("--workload", default="mixed", choices=sorted(WORKLOADS),
                     help="mixed = the headline batch; the others are the single-Morse, 64-Morse, adjoint and "
                          "long-grid cases")
@@ -323,17 +326,17 @@ def main():
     mask = (slot < n_lev[:, None]).to(torch.float64)
 
     def step():
-        db.solve(capi.METHOD_FAST_FP32C, long_window=args.long_window, stream=stream.cuda_stream)
+        db.solve(capi.METHOD_FAST_FP32C, long_window=args.long_window, mid_window=args.mid_window, stream=stream.cuda_stream)
         gE = 2.0 * w * (torch.nan_to_num(db.energy) - target) * mask
         db.adjoint(gE, stream=stream.cuda_stream)
 
-    db.solve(capi.METHOD_FAST_FP32C, long_window=args.long_window, tune=True, stream=stream.cuda_stream)  # autotune the scan shape
+    db.solve(capi.METHOD_FAST_FP32C, long_window=args.long_window, mid_window=args.mid_window, tune=True, stream=stream.cuda_stream)  # autotune the scan shape
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
 
     # stage timing of one instrumented solve (per-kernel events on the solve stream)
-    db.solve(capi.METHOD_FAST_FP32C, long_window=args.long_window, stage_timing=True, stream=stream.cuda_stream)
+    db.solve(capi.METHOD_FAST_FP32C, long_window=args.long_window, mid_window=args.mid_window, stage_timing=True, stream=stream.cuda_stream)
     st = ctx.stats()
     torch.cuda.synchronize()
 
@@ -384,7 +387,7 @@ def main():
 
     def e2e_step():
         sol = ctx.solve(batch_host, b.r_min, b.r_max, b.mu, b.e_cap, b.n_trial, method=capi.METHOD_FAST_FP32C,
-                        level_capacity=cap, keep_psi=True, long_window=args.long_window, out=res_buf)
+                        level_capacity=cap, keep_psi=True, long_window=args.long_window, mid_window=args.mid_window, out=res_buf)
         np.subtract(np.nan_to_num(sol.energy), target_np, out=gE_pinned)
         np.multiply(gE_pinned, w2m, out=gE_pinned)
         return sol, gE_pinned, ctx.adjoint(gE_pinned, Vcat.size, recompute=False, out=gV_pinned.numpy())

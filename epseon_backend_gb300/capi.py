@@ -44,6 +44,9 @@ class Batch(C.Structure):
     ]
 
 
+ALLOC_FN = C.CFUNCTYPE(C.c_void_p, C.c_int64, C.c_void_p)
+
+
 class Opts(C.Structure):
     _fields_ = [
         ("method", C.c_int32),
@@ -54,6 +57,9 @@ class Opts(C.Structure):
         ("long_window", C.c_int32),
         ("wait_polls", C.c_int32),
         ("max_iter", C.c_int32),
+        ("mid_window", C.c_int32),
+        ("psi_alloc", ALLOC_FN),
+        ("psi_alloc_user", C.c_void_p),
     ]
 
 
@@ -331,13 +337,15 @@ class Context:
         wait_polls: int = 0,
         max_iter: int = 0,
         check: bool = True,
+        mid_window: int = 0,
     ) -> Solution:
         """Solve a batch of host potentials (host buffers through the C ABI).
 
         out: a Solution of this batch's shape whose result arrays are written
         in place (for instance page-locked buffers reused across solves, so
         the device-to-host copies run at full speed); its psi is not used.
-        wait_polls / max_iter: epscu_opts bounds (0: the defaults).
+        wait_polls / max_iter: epscu_opts bounds (0: the defaults); mid_window:
+        the warp-per-level tier's threshold (0: default, < 0: off).
         check=False returns the Solution with the status code in .rc instead
         of raising on a non-zero code."""
         V, offsets, N = concat(Vs)
@@ -392,7 +400,7 @@ class Context:
         )
         flags = (WANT_PSI if want_psi else 0) | (KEEP_PSI if keep_psi and not want_psi else 0)
         o = Opts(int(method), flags, float(tol), None, 1 if tune else 0, int(long_window), int(wait_polls),
-                 int(max_iter))
+                 int(max_iter), int(mid_window))
         rc = self._lib.epscu_solve(self._h, C.byref(b), C.byref(r), C.byref(o))
         if check:
             _check(rc)
@@ -489,7 +497,7 @@ class DeviceBatch:
         return C.cast(C.c_void_p(t.data_ptr()), ty) if t is not None else None
 
     def solve(self, method: int = METHOD_FAST_FP32C, tune: bool = False, stage_timing: bool = False, stream=None,
-              long_window: int = 0):
+              long_window: int = 0, mid_window: int = 0):
         import torch
 
         b = Batch(self.n, self._ptr(self.V, _dp), _l(self.offsets), _i(self.N), _d(self.r_min), _d(self.r_max),
@@ -500,7 +508,7 @@ class DeviceBatch:
                    _l(self.psi_offsets), 0)
         flags = MEM_DEVICE | (WANT_PSI if self.want_psi else 0) | (STAGE_TIMING if stage_timing else 0)
         s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
-        o = Opts(int(method), flags, 1e-12, C.c_void_p(s), 1 if tune else 0, int(long_window))
+        o = Opts(int(method), flags, 1e-12, C.c_void_p(s), 1 if tune else 0, int(long_window), 0, 0, int(mid_window))
         _check(self.ctx._lib.epscu_solve(self.ctx.handle, C.byref(b), C.byref(r), C.byref(o)))
         self.psi_required = r.psi_required
 

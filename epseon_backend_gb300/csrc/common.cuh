@@ -71,8 +71,10 @@ struct Header {
     int32_t fallbacks;      // levels that needed the bisection fallback
     int32_t n_units;        // warp work units (<= 32 levels of one potential)
     int32_t n_twist;        // levels handed to the twist-index search
-    int32_t queue[12];      // work-queue heads of the per-level kernels
+    int32_t queue[14];      // work-queue heads of the per-level kernels
     int32_t n_long;         // levels whose window takes the CTA-per-level passes
+    int32_t n_mid;          // levels whose window takes the warp-per-level passes
+    int32_t pad_mid;
     int32_t n_redo;         // norm passes redone at E + dE
     unsigned long long scan_updates;    // point-updates the windowed FP32 scan performed
     unsigned long long refine_updates;  // point-updates of the FP32 refinement passes
@@ -90,13 +92,15 @@ struct Header {
 
 // queue ids of the per-level kernels
 enum { kQRefine32 = 0, kQNewtonDF, kQNormDF, kQWriteDF, kQBisect64, kQNorm64, kQWrite64, kQLongRefine, kQFallback,
-       kQNormLong, kQTwistLong };
+       kQNormLong, kQTwistLong, kQMidRefine, kQNormMid };
 
 // internal level flags (not reported: gather keeps the public bits only)
 // the Newton stage handed the level to the fallback
 #define EPSCU_STATUS_FALLBACK 0x10000
 // the level's passes run one CTA per level (longwin.cu)
 #define EPSCU_STATUS_LONG 0x20000
+// the level's double-float passes run one warp per level (the middle tier, longwin.cu)
+#define EPSCU_STATUS_MID 0x40000
 #define EPSCU_STATUS_PUBLIC 0xffff
 // spacing of the samples of the twist-index search
 constexpr int kTwistSample = 64;

@@ -25,6 +25,10 @@ namespace epscu {
 constexpr int kLongWindow = 8192;
 constexpr int kLongWindowLevels = 60000;
 constexpr int kMinLongWindow = 1024;
+// windows above this many points (and up to the long-window threshold) run
+// their double-float passes one warp per level, after the lane FP32
+// refinement (DevBatch::mid_window overrides it; < 0 turns the tier off)
+constexpr int kMidWindow = 1024;
 
 __host__ __device__ __forceinline__ int default_long_window(int total_levels) {
     int w = kMinLongWindow;
@@ -32,7 +36,11 @@ __host__ __device__ __forceinline__ int default_long_window(int total_levels) {
     return w;
 }
 
-__device__ __forceinline__ bool is_long(const LevelWork& w) { return (w.status & EPSCU_STATUS_LONG) != 0; }
+// the level runs its double-float passes on a group of warps (CTA or warp
+// per level), not on a lane
+__device__ __forceinline__ bool is_long(const LevelWork& w) {
+    return (w.status & (EPSCU_STATUS_LONG | EPSCU_STATUS_MID)) != 0;
+}
 
 // match points stay inside the level's window, off its two end points
 __device__ __forceinline__ int clamp_k(const LevelWork& w, int k) { return max(w.j0 + 1, min(k, w.j1 - 1)); }

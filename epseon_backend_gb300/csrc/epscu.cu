@@ -71,7 +71,7 @@ struct epscu_ctx {
     int sm_count = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;  // the long levels' branch of the fast pipeline
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_zero = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     size_t block = size_t(64) << 20;
     std::map<std::string, DevBuf> bufs;
     std::map<std::string, std::pair<void*, size_t>> pinned;
@@ -108,7 +108,6 @@ struct epscu_ctx {
         if (ev_out) cudaEventDestroy(ev_out);
         if (ev_fork) cudaEventDestroy(ev_fork);
         if (ev_join) cudaEventDestroy(ev_join);
-        if (ev_zero) cudaEventDestroy(ev_zero);
         if (stream2) cudaStreamDestroy(stream2);
         if (stream) cudaStreamDestroy(stream);
     }
@@ -238,7 +237,6 @@ epscu_status epscu_create(int32_t device_ordinal, epscu_ctx** out) {
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_out, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_zero, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         delete c;
         return fail(EPSCU_ERR_CUDA, std::string("context set-up: ") + cudaGetErrorString(e));
@@ -330,22 +328,24 @@ void enqueue_pipeline(epscu_ctx* ctx, const DevBatch& b, int method, bool want_p
     } else {
         launch_window(b, ctx->sm_count, s);
         if (!stage_events) {
-            // the long levels (one CTA each) and the lane levels are disjoint:
-            // the two branches run side by side, the CTA branch filling the SMs
-            // the lane kernels leave idle as their warps drain
-            // (the psi rows are zeroed there too, an HBM stream beside the
-            // compute-bound refinement, before norm_df writes into them)
+            // the long levels (one CTA each), the middle levels (FP32 on lanes,
+            // then one warp each) and the lane levels are disjoint: the CTA
+            // branch runs beside the other two, filling the SMs the per-level
+            // kernels leave idle as they drain (the psi rows are zeroed outside
+            // the level windows there too, an HBM stream beside the
+            // compute-bound refinement; the norm passes write only inside the
+            // windows, so they need not wait for it)
             cudaEventRecord(ctx->ev_fork, s);
             cudaStreamWaitEvent(ctx->stream2, ctx->ev_fork, 0);
             launch_refine32(b, ctx->sm_count, s);
             if (want_psi) launch_zero_psi(b, ctx->sm_count, ctx->stream2);
-            cudaEventRecord(ctx->ev_zero, ctx->stream2);
             launch_refine_long(b, ctx->sm_count, ctx->stream2);
             launch_norm_long(b, ctx->sm_count, ctx->stream2);
             cudaEventRecord(ctx->ev_join, ctx->stream2);
+            launch_refine_mid(b, ctx->sm_count, s);
             launch_newton_df(b, ctx->sm_count, s);
             launch_fallback_long(b, ctx->sm_count, s);
-            cudaStreamWaitEvent(s, ctx->ev_zero, 0);
+            launch_norm_mid(b, ctx->sm_count, s);
             launch_norm_df(b, ctx->sm_count, s);
             cudaStreamWaitEvent(s, ctx->ev_join, 0);
             launch_twist_long(b, ctx->sm_count, s);
@@ -356,11 +356,13 @@ void enqueue_pipeline(epscu_ctx* ctx, const DevBatch& b, int method, bool want_p
             launch_refine_long(b, ctx->sm_count, s);
             rec(9);
             rec(3);
+            launch_refine_mid(b, ctx->sm_count, s);
             launch_newton_df(b, ctx->sm_count, s);
             launch_fallback_long(b, ctx->sm_count, s);
             rec(10);
             if (want_psi) launch_zero_psi(b, ctx->sm_count, s);
             rec(11);
+            launch_norm_mid(b, ctx->sm_count, s);
             launch_norm_df(b, ctx->sm_count, s);
             launch_norm_long(b, ctx->sm_count, s);
             launch_twist_long(b, ctx->sm_count, s);
@@ -396,6 +398,9 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     // host buffers, no psi buffer, psi kept in device memory for the adjoint:
     // the psi size is read back after the level setup, then the rest runs
     const bool keep_psi = (opts.flags & EPSCU_KEEP_PSI) && !want_psi && !dev;
+    // device buffers, no psi buffer, an allocator: psi sized exactly after the
+    // level setup, in the caller's memory
+    const bool alloc_psi = dev && (opts.flags & EPSCU_WANT_PSI) && !res->psi && opts.psi_alloc != nullptr;
     // per-stage events (one stream, stages in sequence) only when asked for;
     // otherwise the fast method's two branches run side by side, graph-replayed
     // for device-resident inputs and launched directly for host buffers
@@ -473,6 +478,7 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     b.order = (int32_t*)ctx->get("order", sizeof(int32_t) * n, &ce);
     b.scan_win = nullptr;
     b.long_list = nullptr;
+    b.mid_list = nullptr;
     b.bis_list = nullptr;
     b.bis_n = nullptr;
     b.Mpre = nullptr;
@@ -483,6 +489,8 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
         if (!b.Mpre || !b.Bmin) return fail(EPSCU_ERR_NOMEM, "device arena (window bounds)");
         b.long_list = (int32_t*)ctx->get("long_list", sizeof(int32_t) * lv, &ce);
         if (!b.long_list) return fail(EPSCU_ERR_NOMEM, "device arena (long list)");
+        b.mid_list = (int32_t*)ctx->get("mid_list", sizeof(int32_t) * lv, &ce);
+        if (!b.mid_list) return fail(EPSCU_ERR_NOMEM, "device arena (middle list)");
         const size_t nb = (size_t)(batch->n_trial + kScanWinBlock - 1) / kScanWinBlock;
         b.scan_win = (int2*)ctx->get("scan_win", sizeof(int2) * (size_t)n * nb, &ce);
         if (!b.scan_win) return fail(EPSCU_ERR_NOMEM, "device arena (scan windows)");
@@ -519,6 +527,7 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     b.tol = opts.tol;
     b.long_window = opts.long_window > 0 ? opts.long_window : 0;  // 0: chosen from the level count
     b.wait_polls = opts.wait_polls;  // 0: the default bound; < 0: the failure self-test
+    b.mid_window = opts.mid_window;  // 0: the default middle-tier threshold; < 0: no middle tier
     b.max_iter = opts.max_iter > 0 ? opts.max_iter : 0;            // 0: the default caps
     b.psi = nullptr;
     b.psi_capacity = 0;
@@ -595,7 +604,7 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     }
 
     // ---- the pipeline (graph-replayed when the device-resident inputs repeat)
-    const bool use_graph = dev && !stage_events;
+    const bool use_graph = dev && !stage_events && !alloc_psi;
     char keybuf[512];
     std::string keybuf_extra;
     std::snprintf(keybuf, sizeof(keybuf), "%d|%d|%d|%d|%p|%p|%p|%p|%p|%p|%p|%p|%lld|%d|%d|%d|%d|%d|%g|%p", n,
@@ -603,7 +612,8 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
                   (void*)o_e, (void*)o_nt, (void*)o_no, (void*)o_nd, (void*)o_st, (void*)o_err,
                   (long long)b.psi_capacity, method, cap, shape.threads, shape.tile, shape.stages, opts.tol,
                   (void*)s);  // s is the context's own stream
-    keybuf_extra = std::to_string(b.long_window);
+    keybuf_extra = std::to_string(b.long_window) + "|" + std::to_string(b.mid_window) + "|" +
+                   std::to_string(b.wait_polls) + "|" + std::to_string(b.max_iter);
     const std::string gkey = std::string(keybuf) + "|" + std::to_string(total_points) + "|" + keybuf_extra;
 
     auto enqueue_inputs = [&]() -> cudaError_t {
@@ -650,17 +660,24 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
         EPSCU_CU(cudaEventRecord(ctx->ev[0], s));
         EPSCU_CU(cudaGraphLaunch(ctx->graph, s));
         EPSCU_CU(cudaEventRecord(ctx->ev[6], s));
-    } else if (keep_psi) {
+    } else if (keep_psi || alloc_psi) {
         if (!stage_events) EPSCU_CU(cudaEventRecord(ctx->ev[0], s));
         EPSCU_CU(enqueue_inputs());
         enqueue_pipeline(ctx, b, method, true, shape, stage_events, s, 1);
         EPSCU_CU(cudaMemcpyAsync(hh, b.hdr, sizeof(Header), cudaMemcpyDeviceToHost, s));
         EPSCU_CU(cudaStreamSynchronize(s));
         const int64_t need = std::max<int64_t>(1, hh->psi_total);
-        b.psi = (double*)ctx->get("psi_keep", sizeof(double) * (size_t)need, &ce);
-        if (!b.psi) return fail(EPSCU_ERR_NOMEM, "device arena (kept psi)");
-        b.psi_capacity = need;
-        enqueue_pipeline(ctx, b, method, true, shape, stage_events, s, 2);
+        if (keep_psi) {
+            b.psi = (double*)ctx->get("psi_keep", sizeof(double) * (size_t)need, &ce);
+            if (!b.psi) return fail(EPSCU_ERR_NOMEM, "device arena (kept psi)");
+            b.psi_capacity = need;
+        } else {
+            b.psi = static_cast<double*>(opts.psi_alloc(need * (int64_t)sizeof(double), opts.psi_alloc_user));
+            b.psi_capacity = b.psi ? need : 0;
+            res->psi = b.psi;
+            res->psi_capacity = b.psi_capacity;
+        }
+        enqueue_pipeline(ctx, b, method, b.psi != nullptr, shape, stage_events, s, 2);
         launch_gather(b, o_nt, o_no, o_e, o_nd, o_st, o_err, method == EPSCU_METHOD_FAST_FP32C ? 1 : 0, s);
         EPSCU_CU(cudaEventRecord(ctx->ev[6], s));
         EPSCU_CU(cudaGetLastError());
@@ -739,20 +756,21 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     st.fallbacks = hh->fallbacks;
     st.twist_searches = hh->n_twist;
     st.norm_redos = hh->n_redo;
-    st.psi_bytes = (want_psi || keep_psi) ? psi_total * 8 : 0;
+    const bool psi_on = want_psi || keep_psi || (alloc_psi && b.psi);
+    st.psi_bytes = psi_on ? psi_total * 8 : 0;
     // plain: prepare, scan64, level/unit setup, bracket, bisect64, norm64,
     // twist64, gather (+ write64); fast: prepare, scan window, scan32, level/unit
-    // setup, bracket, window, refine32, refine_long, newton_df, fallback
-    // (refine_long over the fallback list), norm_df, norm_long, twist_long,
-    // gather (+ zero_psi, scale_psi)
-    const bool psi_kernels = want_psi || keep_psi;
-    st.kernel_launches = method == EPSCU_METHOD_FAST_FP32C ? 15 + (psi_kernels ? 2 : 0) : 9 + (psi_kernels ? 1 : 0);
+    // setup, bracket, window, refine32, refine_long, refine_mid, newton_df,
+    // fallback (refine_long over the fallback list), norm_mid, norm_df,
+    // norm_long, twist_long, gather (+ zero_psi, scale_psi)
+    const bool psi_kernels = psi_on;
+    st.kernel_launches = method == EPSCU_METHOD_FAST_FP32C ? 17 + (psi_kernels ? 2 : 0) : 9 + (psi_kernels ? 1 : 0);
     if (b.bis_list) st.kernel_launches += 6;  // three plan + count rounds after the coarse scan32
     if (method == EPSCU_METHOD_PLAIN_FP64) {
         st.refine_point_updates = 0;
         int64_t bis = 0;
         for (int p = 0; p < n; ++p) bis += (int64_t)std::max(0, hm[p].i1 - hm[p].i0) * hm[p].n_out * hm[p].n_bisect;
-        st.fp64_point_updates = scan_pts + bis + lvl_pts * (want_psi ? 2 : 1);
+        st.fp64_point_updates = scan_pts + bis + lvl_pts * (psi_on ? 2 : 1);
     } else {
         // counted by the kernels over the level windows (algorithmic
         // point-updates: the long-window passes do ~3x this on 256 threads)
@@ -772,7 +790,7 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     ctx->last = b;
     ctx->have_last = true;
     ctx->last_method = method;
-    ctx->last_psi = (want_psi || keep_psi) && hh->error == 0;
+    ctx->last_psi = psi_on && hh->error == 0;
     ctx->last_offsets_dev = d_off;
     ctx->last_total_points = total_points;
     ctx->last_psi_total = psi_total;

@@ -34,6 +34,7 @@ struct DevBatch {
     int32_t* order;            // [n] potentials by decreasing cost
     int2* scan_win;            // [n * ceil(n_trial / kScanWinBlock)] scan windows, or nullptr (full grid)
     int32_t* long_list;        // [max_levels] slots with long windows (CTA-per-level passes), or nullptr
+    int32_t* mid_list;         // [max_levels] slots with middle windows (warp-per-level passes), or nullptr
     int32_t* bis_list;         // [n * n_trial] trial indices of the bisection scan's current round, or
                                // nullptr (every trial energy scanned)
     int32_t* bis_n;            // [n] entries of bis_list per potential
@@ -44,6 +45,7 @@ struct DevBatch {
     int32_t min_level, max_level;
     int32_t max_N;             // longest grid of the batch
     int32_t long_window;       // window length above which a level takes the CTA passes
+    int32_t mid_window;        // window length above which a level takes the warp passes (< 0: none)
     int32_t wait_polls;        // polls of a bounded wait on a staged scan tile (0: kWaitPolls)
     int32_t max_iter;          // cap on FP32 refinement passes (0: 48; fallback passes: twice it)
     double tol;
@@ -116,6 +118,8 @@ void launch_fallback_long(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_norm_long(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_write_long(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_twist_long(const DevBatch& b, int sm_count, cudaStream_t s);
+void launch_refine_mid(const DevBatch& b, int sm_count, cudaStream_t s);
+void launch_norm_mid(const DevBatch& b, int sm_count, cudaStream_t s);
 
 // adjoint.cu
 void launch_adjoint(const DevBatch& b, const double* dL_dE, double* dL_dV, int64_t total_points,

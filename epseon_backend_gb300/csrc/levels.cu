@@ -318,7 +318,8 @@ __global__ void __launch_bounds__(kLevelThreads, 4) refine32_kernel(DevBatch b) 
         if ((int)(threadIdx.x & 31) >= unit.y) continue;
         const int slot = unit.x + (threadIdx.x & 31);
         LevelWork w = b.levels[slot];
-        if ((w.status & EPSCU_STATUS_NOTFOUND) || is_long(w)) continue;  // long windows: refine_long
+        // long windows: refine_long (middle windows take their FP32 passes here)
+        if (w.status & (EPSCU_STATUS_NOTFOUND | EPSCU_STATUS_LONG)) continue;
         if (cancelled(b)) {
             b.levels[slot].status = w.status | EPSCU_STATUS_CANCELLED;
             continue;

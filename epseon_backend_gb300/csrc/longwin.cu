@@ -1,12 +1,14 @@
-// longwin.cu -- the fast method's per-level passes for long windows.
+// longwin.cu -- the fast method's per-level passes on groups of warps.
 //
-// A level whose window holds more than kLongWindow points (a long grid: the
-// 2^20-point Morse has windows of 10^5 - 4.7 10^5 points) cannot be marched
-// by one lane: a pass would cost ~10^6 dependent steps of latency while most
-// of the GPU idles.  Such a level takes one CTA of kLongThreads threads
-// instead.  Each side of a pass (outward from j0 to the match point k, inward
-// from j1 to k) is split into one contiguous chunk per thread and the
-// double-float difference-form recurrence
+// A level whose window is long (a long grid: the 2^20-point Morse has windows
+// of 10^5 - 4.7 10^5 points; on the mixed batch every window above a few
+// thousand points) cannot be marched by one lane: a pass would cost ~10^4 -
+// 10^6 dependent steps of latency while most of the GPU idles.  Such a level
+// takes a group of NW warps instead: the whole CTA (NW = 8) for the longest
+// windows, or one warp (NW = 1) for the middle tier.  Each side of a pass
+// (outward from j0 to the match point k, inward from j1 to k) is split into
+// one contiguous chunk per thread of the group and the double-float
+// difference-form recurrence
 //     D' = D + T (D - 12 A),   A' = A + (T A + D')
 // runs in three phases:
 //   1. every thread marches the two unit states (A, D) = (1, 0) and (0, 1)
@@ -14,28 +16,37 @@
 //      columns of the chunk's 2x2 transfer matrix (with the product of 1/f
 //      over the chunk for the passes that need psi);
 //   2. a parallel prefix scan of the transfer matrices -- Hillis-Steele over
-//      the 32 lanes of each warp with shuffles, then over the warps through
-//      shared memory -- gives the exact starting state and scale of every
-//      chunk;
+//      the 32 lanes of each warp with shuffles, then over the group's warps
+//      through shared memory -- gives the exact starting state and scale of
+//      every chunk;
 //   3. every thread re-runs its chunk from that state: node counts, the sum
-//      of psi^2, the peak of |psi| or the psi write, reduced over the CTA.
-// A pass costs about three serial marches of point-updates, spread over
-// kLongThreads threads.  The matrices span exponential growth, so every
-// product is renormalised by a power of two with the exponent carried in an
-// int; the physical solution is the growing one on both sides (each side runs
-// from a forbidden region towards the match point at the peak of |psi|), so a
+//      of psi^2, the peak of |psi| or the psi write, reduced over the group.
+// A pass costs about three serial marches of point-updates, spread over the
+// group.  The matrices span exponential growth, so every product is
+// renormalised by a power of two with the exponent carried in an int; the
+// physical solution is the growing one on both sides (each side runs from a
+// forbidden region towards the match point at the peak of |psi|), so a
 // product applied to the starting state loses nothing to the discarded
 // subdominant solution.
 //
-// Kernels (one CTA per long level, levels taken from a device queue over the
-// long list the window kernel fills; the lane-per-level kernels skip these
-// levels):
+// FP64 runs once per pass, in the group's thread 0 (the leader): the sums are
+// reduced over the warps in FP32 (FP32 passes) or double-float (double-float
+// passes) with their binary exponents aligned, and the leader forms the
+// side's sum in FP64, the matching function gamma_k, the psi^2 sum and the
+// Cooley step, and hands the pass's result to the group through shared
+// memory.  (Every thread doing that FP64 work kept the FP64 pipe, 1/62 of the
+// FP32 rate on GB300, busy for a large part of a pass on windows of a few
+// thousand points per CTA.)
+//
+// Kernels (one group per level, levels taken from a device queue over a list
+// the window kernel fills; the lane-per-level kernels skip these levels):
 //   refine_long : from the scan bracket, FP32 passes (the same three phases
 //                 in FP32, long_side32) to 2e-9, then double-float
 //                 state-only Newton to 1e-12 (replaces refine32 + newton_df);
 //                 run again over the levels newton_df could not settle (the
 //                 fallback: any window length, full double-float passes from
-//                 the scan bracket widened by one trial spacing);
+//                 the scan bracket widened by one trial spacing), and over
+//                 the middle list from the lane FP32 refinement's result;
 //   norm_long   : the norm pass and its match-point candidates (as norm_df),
 //                 storing psi-hat as tagged float pairs for scale_psi;
 //   twist_long  : the twist-index search for the levels the norm passes flag;
@@ -137,21 +148,136 @@ __device__ __forceinline__ void df_step(dfl T, dfl& A, dfl& D) {
     A = df_add(A, df_add(df_mul(T, A), D));
 }
 
-struct LongShared {
-    Mat2 wtot[kLongWarps], wpre[kLongWarps];
-    Scal qtot[kLongWarps], qpre[kLongWarps];
-    int nodes[kLongWarps];
-    double S[kLongWarps];
-    int pk_L[kLongWarps], pk_s[kLongWarps];
+// ---------------------------------------------------------------- groups
+// A level's passes run on a group of NW warps (NW = 8: the whole CTA of
+// kLongThreads; NW = 1: one warp, kLongThreads / 32 groups per CTA).  The
+// group's thread 0 is its leader.
+template <int NW>
+struct Grp {
+    static constexpr int kThreads = 32 * NW;
+    // thread in the group, lane, warp in the group, group in the CTA (read
+    // from threadIdx each time: nothing held in registers)
+    __device__ __forceinline__ int t() const { return (int)(threadIdx.x % kThreads); }
+    __device__ __forceinline__ int lane() const { return (int)(threadIdx.x & 31); }
+    __device__ __forceinline__ int warp() const { return (int)((threadIdx.x % kThreads) >> 5); }
+    __device__ __forceinline__ int g() const { return (int)(threadIdx.x / kThreads); }
+    __device__ __forceinline__ bool leader() const { return t() == 0; }
+};
+
+template <int NW>
+__device__ __forceinline__ void gsync() {
+    static_assert(NW == 1 || NW == kLongWarps, "a group is one warp or the whole CTA");
+    if constexpr (NW == 1) __syncwarp();
+    else __syncthreads();
+}
+
+// the leader's value to the whole group (slot: the group's shared word)
+template <int NW>
+__device__ __forceinline__ int grp_bcast(const Grp<NW>& G, int v, int& slot) {
+    if constexpr (NW == 1) {
+        return __shfl_sync(0xffffffffu, v, 0);
+    } else {
+        if (G.leader()) slot = v;
+        __syncthreads();
+        const int r = slot;
+        __syncthreads();  // every thread has read the slot
+        return r;
+    }
+}
+
+// the next entry of a device queue for the group
+template <int NW>
+__device__ __forceinline__ int grp_next(const Grp<NW>& G, int* queue, int& slot) {
+    int q = 0;
+    if (G.leader()) q = atomicAdd(queue, 1);
+    return grp_bcast<NW>(G, q, slot);
+}
+
+// A non-negative sum (h + l) 2^e in double-float, and its warp-wide total:
+// each lane's value aligned to the largest exponent of the warp (exact
+// power-of-two scalings), then added with shuffles.  Lane 0's result is the
+// one used (the butterfly's order is fixed, so it is reproducible).
+struct DfE {
+    dfl v;
+    int e;
+};
+
+__device__ __forceinline__ DfE warp_sum_dfe(DfE x) {
+    const bool has = x.v.h > 0.0f;
+    int em = has ? x.e : -(1 << 30);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) em = max(em, __shfl_xor_sync(0xffffffffu, em, o));
+    dfl v = {0.0f, 0.0f};
+    if (has) {
+        const int d = x.e - em;
+        if (d > -120) v = df_scale(x.v, fpow2(d));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v = df_add(v, {__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o)});
+    return {v, em};
+}
+
+// The same for FP32 sums v 2^e.
+struct FE {
+    float v;
+    int e;
+};
+
+__device__ __forceinline__ FE warp_sum_fe(FE x) {
+    const bool has = x.v > 0.0f;
+    int em = has ? x.e : -(1 << 30);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) em = max(em, __shfl_xor_sync(0xffffffffu, em, o));
+    float v = 0.0f;
+    if (has) {
+        const int d = x.e - em;
+        if (d > -120) v = x.v * fpow2(d);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return {v, em};
+}
+
+// a thread's SqSum (in units of 2^e0) as a DfE; the FP64 spill is rare
+__device__ __forceinline__ DfE sqsum_dfe(const SqSum& ss, int e0) {
+    if (ss.x == 0.0) return {ss.d, e0};
+    const double v = ss.value();
+    if (!(v > 0.0) || !isfinite(v)) return {{0.0f, 0.0f}, e0};
+    const int ex = exp_of(v);
+    return {df_from_double(v * pow2(-ex)), e0 + ex};
+}
+
+// (h + l) 2^e in FP64 (the leader's combine)
+__device__ __forceinline__ double dfe_to_double(DfE x) {
+    if (!(x.v.h > 0.0f)) return 0.0;
+    return (f2d(x.v.h) + f2d(x.v.l)) * pow2(max(-1000, min(1000, x.e)));
+}
+
+// ------------------------------------------------------- double-float sides
+template <int NW>
+struct SharedDF {
+    Mat2 wtot[NW], wpre[NW];
+    Scal qtot[NW], qpre[NW];
+    int nodes[NW];
+    DfE s[NW];  // warp partial sums of psi-hat^2, absolute exponents
+    int pk_L[NW], pk_s[NW];
+    double gb[NW];  // MODE 5: warp minima of |gamma| and their points
+    int gk[NW];
     // the side's final state (written by the thread holding the last chunk)
     dfl A, D, q;
     int eA, eQ;
+    // the leader's broadcasts: the pass energy and the pass result
+    dfl aE;
+    PassDF res;
+    int word;  // grp_bcast / grp_next slot
 };
 
 // One side of a pass over steps 0..nsteps-1 (point from + dir * step), the
-// CTA-parallel twin of side_df<MODE>: the same outputs in the same scales
+// group-parallel twin of side_df<MODE>: the same outputs in the same scales
 // (state and psi-hat at the end with their exponents, S relative to the
-// final scale, peak in absolute log2).  Called by every thread of the CTA.
+// final scale, peak in absolute log2), valid in the leader.  Called by every
+// thread of the group.
 template <int MODE>
 struct LongSide {
     dfl A, D, q;
@@ -163,7 +289,8 @@ struct LongSide {
 
 // The twist-index search (MODE 4: outward sweep storing the sampled ratios,
 // MODE 5: inward sweep forming |gamma_k| at the same samples) reuses the
-// state-only chunked march; this is its scratch and result.
+// state-only chunked march; this is its scratch and result (the result is
+// handed to every thread of the group).
 struct TwistIO {
     double* rho;        // sampled outward ratios (one every kTwistSample points from j0)
     const double* W;    // a V (FP64) of the potential
@@ -173,18 +300,19 @@ struct TwistIO {
     int k;              //   and its point
 };
 
-template <int MODE>
-__device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int from, int to, int dir,
-                                    double* __restrict__ out, double L, int Xk, LongShared& sh,
+template <int NW, int MODE>
+__device__ LongSide<MODE> long_side(const Grp<NW>& G, const float2* __restrict__ Wf, dfl aE, int from, int to,
+                                    int dir, double* __restrict__ out, double L, int Xk, SharedDF<NW>& sh,
                                     TwistIO* tw = nullptr) {
     // MODE 0: state, 1: + sums/peak, 2: + psi write, 3: MODE 1 + unnormalised
     // psi-hat written in the absolute scale, 4/5: twist sweeps (state)
     constexpr bool kPsi = MODE == 1 || MODE == 2 || MODE == 3;
     constexpr bool kSums = MODE == 1 || MODE == 3;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int kT = Grp<NW>::kThreads;
+    const int tid = G.t(), lane = G.lane(), warp = G.warp();
     const int nsteps = (to - from) * dir;
     LongSide<MODE> res;
-    if (nsteps <= 0) {
+    if (nsteps <= 0) {  // uniform over the group: no barrier is skipped by part of it
         res.A = {1.0f, 0.0f};
         res.D = {1.0f, 0.0f};
         res.q = {1.0f, 0.0f};
@@ -193,9 +321,13 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
         res.S = 0.0;
         res.peak_L = -(1 << 30);
         res.peak_i = from;
+        if (MODE == 5) {
+            tw->best = INFINITY;
+            tw->k = 0x7fffffff;
+        }
         return res;
     }
-    const int len = (nsteps + kLongThreads - 1) / kLongThreads;
+    const int len = (nsteps + kT - 1) / kT;
     const int s0 = min(tid * len, nsteps), s1 = min(s0 + len, nsteps);
 
     // ---- phase 1: this chunk's transfer matrix (and product of 1/f)
@@ -238,30 +370,35 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
             if (kPsi) P = scal_mul(P, py);
         }
     }
-    if (lane == 31) {
-        sh.wtot[warp] = M;
-        sh.qtot[warp] = P;
-    }
-    __syncthreads();
-    if (tid == 0) {
-        Mat2 acc = mat_identity();
-        Scal qa{{1.0f, 0.0f}, 0};
-        for (int w = 0; w < kLongWarps; ++w) {
-            sh.wpre[w] = acc;
-            sh.qpre[w] = qa;
-            acc = mat_mul(sh.wtot[w], acc);
-            if (kPsi) qa = scal_mul(sh.qtot[w], qa);
-        }
-    }
-    __syncthreads();
     Mat2 Mx = shfl_up_mat(M, 1);
     Scal Px = shfl_up_scal(P, 1);
-    if (lane == 0) {
-        Mx = sh.wpre[warp];
-        Px = sh.qpre[warp];
-    } else {
-        Mx = mat_mul(Mx, sh.wpre[warp]);
-        if (kPsi) Px = scal_mul(Px, sh.qpre[warp]);
+    if constexpr (NW > 1) {
+        if (lane == 31) {
+            sh.wtot[warp] = M;
+            sh.qtot[warp] = P;
+        }
+        gsync<NW>();
+        if (tid == 0) {
+            Mat2 acc = mat_identity();
+            Scal qa{{1.0f, 0.0f}, 0};
+            for (int w = 0; w < NW; ++w) {
+                sh.wpre[w] = acc;
+                sh.qpre[w] = qa;
+                acc = mat_mul(sh.wtot[w], acc);
+                if (kPsi) qa = scal_mul(sh.qtot[w], qa);
+            }
+        }
+        gsync<NW>();
+        if (lane == 0) {
+            Mx = sh.wpre[warp];
+            Px = sh.qpre[warp];
+        } else {
+            Mx = mat_mul(Mx, sh.wpre[warp]);
+            if (kPsi) Px = scal_mul(Px, sh.qpre[warp]);
+        }
+    } else if (lane == 0) {
+        Mx = mat_identity();
+        Px = {{1.0f, 0.0f}, 0};
     }
 
     // ---- phase 3: this chunk from its starting state (A, D) = Mx (1, 1)
@@ -281,7 +418,6 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
     int eQ = Px.e;
     PsiTag tag = psi_tag(MODE == 3 ? eA + eQ : 0);  // the stored pairs' scale and tag
     int nodes = 0;
-    double S = 0.0;
     SqSum ss;
     ss.init();
     int peak_L = -(1 << 30), peak_s = 0x7fffffff;
@@ -363,9 +499,7 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
         }
     }
 
-    if (kSums) S = ss.value();
-
-    // ---- reductions over the CTA
+    // ---- reductions: over each warp with shuffles, over the warps by the leader
     const int t_last = (nsteps - 1) / len;
     if (tid == t_last) {
         sh.A = A;
@@ -376,6 +510,7 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) nodes += __shfl_xor_sync(0xffffffffu, nodes, o);
+    DfE sw{{0.0f, 0.0f}, 0};
     if (kSums) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
@@ -386,6 +521,8 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
                 peak_s = s2;
             }
         }
+        // this chunk's sum in the absolute scale 2^(2 (eA + eQ))
+        sw = warp_sum_dfe(s1 > s0 ? sqsum_dfe(ss, 2 * (eA + eQ)) : DfE{{0.0f, 0.0f}, 0});
     }
     if (MODE == 5) {
 #pragma unroll
@@ -397,101 +534,109 @@ __device__ LongSide<MODE> long_side(const float2* __restrict__ Wf, dfl aE, int f
                 g_k = k2;
             }
         }
-        if (lane == 0) {
-            sh.S[warp] = g_best;
-            sh.pk_s[warp] = g_k;
-        }
     }
     if (lane == 0) {
         sh.nodes[warp] = nodes;
-        if (MODE != 5) sh.pk_s[warp] = peak_s;
         sh.pk_L[warp] = peak_L;
-    }
-    __syncthreads();
-    res.A = sh.A;
-    res.D = sh.D;
-    res.q = sh.q;
-    res.eA = sh.eA;
-    res.eQ = sh.eQ;
-    if (kSums) {
-        // this chunk's sum in the side's final scale
-        const int d = 2 * (eA + eQ - (res.eA + res.eQ));
-        double term = (s1 > s0 && d > -1000) ? S * pow2(min(d, 1000)) : 0.0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) term += __shfl_xor_sync(0xffffffffu, term, o);
-        if (lane == 0) sh.S[warp] = term;
-    }
-    __syncthreads();
-    int nsum = 0;
-    double Ssum = 0.0;
-    int pL = -(1 << 30), ps = 0x7fffffff;
-    for (int w = 0; w < kLongWarps; ++w) {
-        nsum += sh.nodes[w];
-        if (kSums) {
-            Ssum += sh.S[w];
-            if (sh.pk_L[w] > pL || (sh.pk_L[w] == pL && sh.pk_s[w] < ps)) {
-                pL = sh.pk_L[w];
-                ps = sh.pk_s[w];
-            }
+        sh.pk_s[warp] = peak_s;
+        if (kSums) sh.s[warp] = sw;
+        if (MODE == 5) {
+            sh.gb[warp] = g_best;
+            sh.gk[warp] = g_k;
         }
     }
-    res.nodes = nsum;
-    res.S = Ssum;
-    res.peak_L = pL;
-    res.peak_i = ps == 0x7fffffff ? from : from + dir * ps;
+    gsync<NW>();
+    if (G.leader()) {
+        res.A = sh.A;
+        res.D = sh.D;
+        res.q = sh.q;
+        res.eA = sh.eA;
+        res.eQ = sh.eQ;
+        int nsum = 0;
+        double Ssum = 0.0;
+        int pL = -(1 << 30), ps = 0x7fffffff;
+        for (int w = 0; w < NW; ++w) {
+            nsum += sh.nodes[w];
+            if (kSums) {
+                // the warp's sum in the side's final scale
+                DfE x = sh.s[w];
+                x.e -= 2 * (res.eA + res.eQ);
+                Ssum += dfe_to_double(x);
+                if (sh.pk_L[w] > pL || (sh.pk_L[w] == pL && sh.pk_s[w] < ps)) {
+                    pL = sh.pk_L[w];
+                    ps = sh.pk_s[w];
+                }
+            }
+        }
+        res.nodes = nsum;
+        res.S = Ssum;
+        res.peak_L = pL;
+        res.peak_i = ps == 0x7fffffff ? from : from + dir * ps;
+    }
     if (MODE == 5) {
+        // every thread of the group takes the search's result
         double gb = INFINITY;
         int gk = 0x7fffffff;
-        for (int w = 0; w < kLongWarps; ++w)
-            if (sh.S[w] < gb || (sh.S[w] == gb && sh.pk_s[w] < gk)) {
-                gb = sh.S[w];
-                gk = sh.pk_s[w];
+        for (int w = 0; w < NW; ++w)
+            if (sh.gb[w] < gb || (sh.gb[w] == gb && sh.gk[w] < gk)) {
+                gb = sh.gb[w];
+                gk = sh.gk[w];
             }
         tw->best = gb;
         tw->k = gk;
     }
-    __syncthreads();  // the shared scratch is reused by the next call
+    // (no barrier here: the next writes of these fields come after the next
+    // call's phase-2 barriers, which the leader reaches only after its reads)
     return res;
 }
 
-// One pass at E with match point k (the CTA twin of pass_df<MODE>, MODE 0/1).
-// MODE 3 also stores the unnormalised psi-hat of the window in row (if not null).
-template <int MODE>
-__device__ PassDF long_pass(const PotMeta& m, const LevelWork& w, const float2* __restrict__ Wf,
-                            const double* __restrict__ W64, double E, int k, double sum_fallback, LongShared& sh,
-                            double* __restrict__ row = nullptr) {
-    const dfl aE = energy_df(m, E);
-    const LongSide<MODE> o = long_side<MODE>(Wf, aE, w.j0, k, +1, row, 0.0, 0, sh);
-    const LongSide<MODE> in = long_side<MODE>(Wf, aE, w.j1, k, -1, row, 0.0, 0, sh);
-    const double Tk = __dsub_rn(__dmul_rn(m.a, E), __ldg(W64 + k));
-    const double fk = 1.0 + Tk;
-    const double Ao = df_to_double(o.A), Do = df_to_double(o.D);
-    const double Ai = df_to_double(in.A), Di = df_to_double(in.D);
-    PassDF r;
-    r.gamma = -12.0 * Tk / fk + Do / Ao + Di / Ai;
-    r.nodes = o.nodes + in.nodes;
-    r.count = r.nodes + (r.gamma < 0.0 ? 1 : 0);
-    r.peak_i = k;
-    r.peak_log2 = 0;
-    r.pk_out = r.pk_in = 0.0;
-    r.ex_out = r.ex_in = 0;
-    if (MODE == 1 || MODE == 3) {
-        const double rfk = 1.0 / fk;
-        r.pk_out = Ao * df_to_double(o.q) * rfk;
-        r.pk_in = Ai * df_to_double(in.q) * rfk;
-        r.ex_out = o.eA + o.eQ;
-        r.ex_in = in.eA + in.eQ;
-        r.sum = o.S / (r.pk_out * r.pk_out) + in.S / (r.pk_in * r.pk_in) + 1.0;
-        const int Lo = (r.pk_out != 0.0 ? exp_of(fabs(r.pk_out)) : -1000) + r.ex_out;
-        const int Li = (r.pk_in != 0.0 ? exp_of(fabs(r.pk_in)) : -1000) + r.ex_in;
-        const int po = o.peak_L - Lo, pi = in.peak_L - Li;
-        r.peak_log2 = max(po, pi);
-        r.peak_i = po >= pi ? o.peak_i : in.peak_i;
-    } else {
-        r.sum = sum_fallback;
+// One pass at E with match point k (the group twin of pass_df<MODE>): the
+// leader turns the two sides into the Cooley correction, the count, the sum
+// and the peak, and hands the result to the group.  MODE 3 also stores the
+// unnormalised psi-hat of the window in row (if not null).
+template <int NW, int MODE>
+__device__ __forceinline__ PassDF long_pass(const Grp<NW>& G, const PotMeta& m, const LevelWork& w,
+                                            const float2* __restrict__ Wf, const double* __restrict__ W64, double E,
+                                            int k, double sum_fallback, SharedDF<NW>& sh,
+                                            double* __restrict__ row = nullptr) {
+    if (G.leader()) sh.aE = energy_df(m, E);
+    gsync<NW>();
+    const dfl aE = sh.aE;
+    const LongSide<MODE> o = long_side<NW, MODE>(G, Wf, aE, w.j0, k, +1, row, 0.0, 0, sh);
+    const LongSide<MODE> in = long_side<NW, MODE>(G, Wf, aE, w.j1, k, -1, row, 0.0, 0, sh);
+    if (G.leader()) {
+        const double Tk = __dsub_rn(__dmul_rn(m.a, E), __ldg(W64 + k));
+        const double fk = 1.0 + Tk;
+        const double Ao = df_to_double(o.A), Do = df_to_double(o.D);
+        const double Ai = df_to_double(in.A), Di = df_to_double(in.D);
+        PassDF r;
+        r.gamma = -12.0 * Tk / fk + Do / Ao + Di / Ai;
+        r.nodes = o.nodes + in.nodes;
+        r.count = r.nodes + (r.gamma < 0.0 ? 1 : 0);
+        r.peak_i = k;
+        r.peak_log2 = 0;
+        r.pk_out = r.pk_in = 0.0;
+        r.ex_out = r.ex_in = 0;
+        if (MODE == 1 || MODE == 3) {
+            const double rfk = 1.0 / fk;
+            r.pk_out = Ao * df_to_double(o.q) * rfk;
+            r.pk_in = Ai * df_to_double(in.q) * rfk;
+            r.ex_out = o.eA + o.eQ;
+            r.ex_in = in.eA + in.eQ;
+            r.sum = o.S / (r.pk_out * r.pk_out) + in.S / (r.pk_in * r.pk_in) + 1.0;
+            const int Lo = (r.pk_out != 0.0 ? exp_of(fabs(r.pk_out)) : -1000) + r.ex_out;
+            const int Li = (r.pk_in != 0.0 ? exp_of(fabs(r.pk_in)) : -1000) + r.ex_in;
+            const int po = o.peak_L - Lo, pi = in.peak_L - Li;
+            r.peak_log2 = max(po, pi);
+            r.peak_i = po >= pi ? o.peak_i : in.peak_i;
+        } else {
+            r.sum = sum_fallback;
+        }
+        r.dE = r.gamma * fk * fk / (12.0 * m.a * r.sum);
+        sh.res = r;
     }
-    r.dE = r.gamma * fk * fk / (12.0 * m.a * r.sum);
-    return r;
+    gsync<NW>();
+    return sh.res;
 }
 
 // ------------------------------------------------------------------ FP32 passes
@@ -561,15 +706,19 @@ __device__ __forceinline__ Scalf shfl_up_scalf(const Scalf& s, int o) {
     return {__shfl_up_sync(0xffffffffu, s.v, o), __shfl_up_sync(0xffffffffu, s.e, o)};
 }
 
-struct LongShared32 {
-    Mat2f wtot[kLongWarps], wpre[kLongWarps];
-    Scalf ftot[kLongWarps], fpre[kLongWarps];
+template <int NW>
+struct Shared32 {
+    Mat2f wtot[NW], wpre[NW];
+    Scalf ftot[NW], fpre[NW];
     Scalf fall;  // product of f^2 over the side
-    int nodes[kLongWarps];
-    double S[kLongWarps];
-    int pk_L[kLongWarps], pk_s[kLongWarps];
+    int nodes[NW];
+    FE s[NW];  // warp partial sums, absolute exponents
+    int pk_L[NW], pk_s[NW];
     float A, D;  // the side's final state (thread holding the last chunk)
     int eA;
+    // the leader's broadcasts: a E as a float pair and the pass result
+    float aEh, aEl;
+    PassDF res;
 };
 
 struct LongSide32 {
@@ -586,13 +735,16 @@ struct LongSide32 {
 // pass accumulates them (S' = f^2 S + A^2 before each step), chunked: phase 1
 // gives each chunk's transfer matrix and product F of f^2, phase 2 scans
 // them, phase 3 re-runs the chunk from its exact start state; a chunk's S is
-// carried to the side's end by the product of F over the later chunks.
-__device__ LongSide32 long_side32(const float2* __restrict__ Wf, float aEh, float aEl, int from, int to, int dir,
-                                  LongShared32& sh) {
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+// carried to the side's end by the product of F over the later chunks.  The
+// result is valid in the leader.
+template <int NW>
+__device__ LongSide32 long_side32(const Grp<NW>& G, const float2* __restrict__ Wf, float aEh, float aEl, int from,
+                                  int to, int dir, Shared32<NW>& sh) {
+    constexpr int kT = Grp<NW>::kThreads;
+    const int tid = G.t(), lane = G.lane(), warp = G.warp();
     const int nsteps = (to - from) * dir;
     LongSide32 res;
-    if (nsteps <= 0) {
+    if (nsteps <= 0) {  // uniform over the group
         res.A = 1.0f;
         res.D = 1.0f;
         res.eA = 0;
@@ -602,7 +754,7 @@ __device__ LongSide32 long_side32(const float2* __restrict__ Wf, float aEh, floa
         res.peak_i = from;
         return res;
     }
-    const int len = (nsteps + kLongThreads - 1) / kLongThreads;
+    const int len = (nsteps + kT - 1) / kT;
     const int s0 = min(tid * len, nsteps), s1 = min(s0 + len, nsteps);
 
     // ---- phase 1: transfer matrix and product of f^2 of this chunk
@@ -651,27 +803,35 @@ __device__ LongSide32 long_side32(const float2* __restrict__ Wf, float aEh, floa
             F = scalf_mul(F, fy);
         }
     }
-    if (lane == 31) {
-        sh.wtot[warp] = M;
-        sh.ftot[warp] = F;
-    }
-    __syncthreads();
-    if (tid == 0) {
-        Mat2f acc = {1.0f, 0.0f, 0.0f, 1.0f, 0};
-        Scalf fa{1.0f, 0};
-        for (int w = 0; w < kLongWarps; ++w) {
-            sh.wpre[w] = acc;
-            sh.fpre[w] = fa;
-            acc = matf_mul(sh.wtot[w], acc);
-            fa = scalf_mul(sh.ftot[w], fa);
-        }
-        sh.fall = fa;
-    }
-    __syncthreads();
     Mat2f Mx = shfl_up_matf(M, 1);
-    if (lane == 0) Mx = sh.wpre[warp];
-    else Mx = matf_mul(Mx, sh.wpre[warp]);
-    const Scalf Fin = scalf_mul(F, sh.fpre[warp]);  // f^2 over chunks 0..tid
+    Scalf Fin = F;  // f^2 over the chunks up to this thread's
+    Scalf Fall;     // f^2 over the side
+    if constexpr (NW > 1) {
+        if (lane == 31) {
+            sh.wtot[warp] = M;
+            sh.ftot[warp] = F;
+        }
+        gsync<NW>();
+        if (tid == 0) {
+            Mat2f acc = {1.0f, 0.0f, 0.0f, 1.0f, 0};
+            Scalf fa{1.0f, 0};
+            for (int w = 0; w < NW; ++w) {
+                sh.wpre[w] = acc;
+                sh.fpre[w] = fa;
+                acc = matf_mul(sh.wtot[w], acc);
+                fa = scalf_mul(sh.ftot[w], fa);
+            }
+            sh.fall = fa;
+        }
+        gsync<NW>();
+        if (lane == 0) Mx = sh.wpre[warp];
+        else Mx = matf_mul(Mx, sh.wpre[warp]);
+        Fin = scalf_mul(F, sh.fpre[warp]);
+        Fall = sh.fall;
+    } else {
+        if (lane == 0) Mx = {1.0f, 0.0f, 0.0f, 1.0f, 0};
+        Fall = {__shfl_sync(0xffffffffu, F.v, 31), __shfl_sync(0xffffffffu, F.e, 31)};
+    }
 
     // ---- phase 3: this chunk from its start state (A, D) = Mx (1, 1)
     float A = Mx.a + Mx.b, D = Mx.c + Mx.d;
@@ -719,7 +879,7 @@ __device__ LongSide32 long_side32(const float2* __restrict__ Wf, float aEh, floa
         }
     }
 
-    // ---- reductions over the CTA
+    // ---- reductions
     const int t_last = (nsteps - 1) / len;
     if (tid == t_last) {
         sh.A = A;
@@ -736,80 +896,95 @@ __device__ LongSide32 long_side32(const float2* __restrict__ Wf, float aEh, floa
             peak_s = s2;
         }
     }
+    // this chunk's S carried to the side's end (times f^2 over the later
+    // chunks = F_all / F_in), in the absolute scale: S (Fall.v / Fin.v)
+    // 2^(2 eA + Fall.e - Fin.e)
+    FE x{0.0f, 0};
+    if (s1 > s0 && S != 0.0f && Fin.v != 0.0f) x = {S * __fdividef(Fall.v, Fin.v), 2 * eA + Fall.e - Fin.e};
+    const FE sw = warp_sum_fe(x);
     if (lane == 0) {
         sh.nodes[warp] = nodes;
         sh.pk_L[warp] = peak_L;
         sh.pk_s[warp] = peak_s;
+        sh.s[warp] = sw;
     }
-    __syncthreads();
-    res.A = sh.A;
-    res.D = sh.D;
-    res.eA = sh.eA;
-    {
-        // this chunk's S carried to the side's end (times f^2 over the later
-        // chunks = F_all / F_in) in units of 2^(2 eA_final)
-        double term = 0.0;
-        if (s1 > s0 && S != 0.0f) {
-            const int d = 2 * (eA - res.eA) + sh.fall.e - Fin.e;
-            if (d > -1000) term = (double)S * ((double)sh.fall.v / (double)Fin.v) * pow2(min(d, 1000));
+    gsync<NW>();
+    if (G.leader()) {
+        res.A = sh.A;
+        res.D = sh.D;
+        res.eA = sh.eA;
+        int nsum = 0;
+        double Ssum = 0.0;
+        int pL = -(1 << 30), ps = 0x7fffffff;
+        for (int w = 0; w < NW; ++w) {
+            nsum += sh.nodes[w];
+            const FE s = sh.s[w];
+            if (s.v > 0.0f) Ssum += (double)s.v * pow2(max(-1000, min(1000, s.e - 2 * res.eA)));
+            if (sh.pk_L[w] > pL || (sh.pk_L[w] == pL && sh.pk_s[w] < ps)) {
+                pL = sh.pk_L[w];
+                ps = sh.pk_s[w];
+            }
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) term += __shfl_xor_sync(0xffffffffu, term, o);
-        if (lane == 0) sh.S[warp] = term;
+        res.nodes = nsum;
+        res.S = Ssum;
+        res.peak_L = pL;
+        res.peak_i = ps == 0x7fffffff ? from : from + dir * ps;
     }
-    __syncthreads();
-    int nsum = 0;
-    double Ssum = 0.0;
-    int pL = -(1 << 30), ps = 0x7fffffff;
-    for (int w = 0; w < kLongWarps; ++w) {
-        nsum += sh.nodes[w];
-        Ssum += sh.S[w];
-        if (sh.pk_L[w] > pL || (sh.pk_L[w] == pL && sh.pk_s[w] < ps)) {
-            pL = sh.pk_L[w];
-            ps = sh.pk_s[w];
-        }
-    }
-    res.nodes = nsum;
-    res.S = Ssum;
-    res.peak_L = pL;
-    res.peak_i = ps == 0x7fffffff ? from : from + dir * ps;
-    __syncthreads();  // the shared scratch is reused by the next call
     return res;
 }
 
-// One FP32 pass at E with match point k (the CTA twin of the lane pass):
-// Cooley correction, count, sum and the peak of |psi| relative to psi_k.
-__device__ PassDF long_pass32(const PotMeta& m, const LevelWork& w, const float2* __restrict__ Wf,
-                              const double* __restrict__ W64, double E, int k, LongShared32& sh) {
-    const double aE = __dmul_rn(m.a, E);
-    const float aEh = __double2float_rn(aE);
-    const float aEl = __double2float_rn(aE - (double)aEh);
-    const LongSide32 o = long_side32(Wf, aEh, aEl, w.j0, k, +1, sh);
-    const LongSide32 in = long_side32(Wf, aEh, aEl, w.j1, k, -1, sh);
-    const double Tk = aE - __ldg(W64 + k);
-    const double fk = 1.0 + Tk;
-    const double uA = o.A, vC = in.A;
-    PassDF r;
-    // gamma_k = -12 T_k / f_k + D_o / u_k + D_i / v_k   (no cancellation)
-    r.gamma = -12.0 * Tk / fk + (double)o.D / uA + (double)in.D / vC;
-    const double fk2 = fk * fk;
-    r.sum = fk2 * (o.S / (uA * uA) + in.S / (vC * vC)) + 1.0;
-    r.dE = r.gamma * fk2 / (12.0 * m.a * r.sum);
-    r.nodes = o.nodes + in.nodes;
-    r.count = r.nodes + (r.gamma < 0.0 ? 1 : 0);
-    const int Lo = o.eA + (o.A != 0.0f ? fexp(fabsf(o.A)) : -1000);
-    const int Li = in.eA + (in.A != 0.0f ? fexp(fabsf(in.A)) : -1000);
-    const int po = o.peak_L - Lo, pi = in.peak_L - Li;
-    r.peak_log2 = max(po, pi);
-    r.peak_i = po >= pi ? o.peak_i : in.peak_i;
-    r.pk_out = r.pk_in = 0.0;
-    r.ex_out = r.ex_in = 0;
-    return r;
+// One FP32 pass at E with match point k (the group twin of the lane pass):
+// Cooley correction, count, sum and the peak of |psi| relative to psi_k,
+// formed by the leader and handed to the group.
+template <int NW>
+__device__ __forceinline__ PassDF long_pass32(const Grp<NW>& G, const PotMeta& m, const LevelWork& w,
+                                              const float2* __restrict__ Wf, const double* __restrict__ W64,
+                                              double E, int k, Shared32<NW>& sh) {
+    if (G.leader()) {
+        const double aE = __dmul_rn(m.a, E);
+        const float aEh = __double2float_rn(aE);
+        sh.aEh = aEh;
+        sh.aEl = __double2float_rn(aE - (double)aEh);
+    }
+    gsync<NW>();
+    const float aEh = sh.aEh, aEl = sh.aEl;
+    const LongSide32 o = long_side32<NW>(G, Wf, aEh, aEl, w.j0, k, +1, sh);
+    const LongSide32 in = long_side32<NW>(G, Wf, aEh, aEl, w.j1, k, -1, sh);
+    if (G.leader()) {
+        const double aE = __dmul_rn(m.a, E);
+        const double Tk = aE - __ldg(W64 + k);
+        const double fk = 1.0 + Tk;
+        const double uA = o.A, vC = in.A;
+        PassDF r;
+        // gamma_k = -12 T_k / f_k + D_o / u_k + D_i / v_k   (no cancellation)
+        r.gamma = -12.0 * Tk / fk + (double)o.D / uA + (double)in.D / vC;
+        const double fk2 = fk * fk;
+        r.sum = fk2 * (o.S / (uA * uA) + in.S / (vC * vC)) + 1.0;
+        r.dE = r.gamma * fk2 / (12.0 * m.a * r.sum);
+        r.nodes = o.nodes + in.nodes;
+        r.count = r.nodes + (r.gamma < 0.0 ? 1 : 0);
+        const int Lo = o.eA + (o.A != 0.0f ? fexp(fabsf(o.A)) : -1000);
+        const int Li = in.eA + (in.A != 0.0f ? fexp(fabsf(in.A)) : -1000);
+        const int po = o.peak_L - Lo, pi = in.peak_L - Li;
+        r.peak_log2 = max(po, pi);
+        r.peak_i = po >= pi ? o.peak_i : in.peak_i;
+        r.pk_out = r.pk_in = 0.0;
+        r.ex_out = r.ex_in = 0;
+        sh.res = r;
+    }
+    gsync<NW>();
+    return sh.res;
 }
 
-__device__ __forceinline__ bool cancelled(const DevBatch& b) { return b.cancel && *b.cancel; }
+// the host-mapped cancel flag, read by the leader and handed to the group
+// (threads that read it separately could see it change between their reads
+// and part at the next barrier)
+template <int NW>
+__device__ __forceinline__ bool grp_cancelled(const Grp<NW>& G, const DevBatch& b, int& slot) {
+    return grp_bcast<NW>(G, G.leader() && b.cancel && *b.cancel ? 1 : 0, slot) != 0;
+}
 
-// Long levels from their scan bracket, in three stages:
+// Levels on groups of warps, in up to three stages:
 //   1. FP32 passes (long_pass32): safeguarded Cooley-Newton to |dE| <= 2e-9
 //      with the count bracket, the match point moved to the peak of |psi|;
 //   2. double-float state-only passes with the FP32 sum as the Newton
@@ -823,42 +998,68 @@ __device__ __forceinline__ bool cancelled(const DevBatch& b) { return b.cancel &
 //      count (so a neighbouring level cannot attract the iteration) and stay
 //      inside the bracket, bisection otherwise.  After the match point moves
 //      to the peak of |psi| the pass is redone at the same E.
-// fallback = 0: the long list (stages 1-3); 1: the levels newton_df handed
-// over (stage 3 only).
+// mode 0: the long list (stages 1-3); 1: the levels newton_df handed over
+// (stage 3 only); 2: the middle list, whose FP32 refinement the lane kernel
+// refine32 did (stage 2 from its energy, bracket, match point and sum, with
+// newton_df's acceptance rule, then stage 3 if it does not settle).  Every
+// thread of a group runs the same control flow on the leader's pass results
+// (the group's passes are collective).
 constexpr double kTol32Long = 2e-9;
 
-__global__ void __launch_bounds__(kLongThreads) refine_long_kernel(DevBatch b, int fallback) {
-    __shared__ LongShared sh;
-    __shared__ LongShared32 sh32;
-    const int n = fallback ? min(b.hdr->fallbacks, b.max_levels) : min(b.hdr->n_long, b.max_levels);
-    const int32_t* list = fallback ? b.fallback_list : b.long_list;
-    __shared__ int s_q;
-    // levels from a device queue (a CTA takes the next as it finishes one)
+template <int NW>
+__global__ void __launch_bounds__(kLongThreads) refine_long_kernel(DevBatch b, int mode, const int32_t* list,
+                                                                   const int32_t* list_len, int qid) {
+    constexpr int kG = kLongThreads / (32 * NW);
+    __shared__ SharedDF<NW> shd[kG];
+    __shared__ Shared32<NW> sh32s[kG];
+    const Grp<NW> G;
+    SharedDF<NW>& sh = shd[G.g()];
+    Shared32<NW>& sh32 = sh32s[G.g()];
+    const int n = min(*list_len, b.max_levels);  // filled on the device earlier in the solve
+    // levels from a device queue (a group takes the next as it finishes one)
     for (;;) {
-        if (threadIdx.x == 0) s_q = atomicAdd(&b.hdr->queue[fallback ? kQFallback : kQLongRefine], 1);
-        __syncthreads();
-        const int q = s_q;
-        __syncthreads();  // every thread has read s_q
+        const int q = grp_next<NW>(G, &b.hdr->queue[qid], sh.word);
         if (q >= n) break;
         const int slot = list[q];
         LevelWork w = b.levels[slot];
         if (w.status & EPSCU_STATUS_NOTFOUND) continue;
-        if (cancelled(b)) {
-            if (threadIdx.x == 0) b.levels[slot].status = w.status | EPSCU_STATUS_CANCELLED;
+        if (grp_cancelled<NW>(G, b, sh.word)) {
+            if (G.leader()) b.levels[slot].status = w.status | EPSCU_STATUS_CANCELLED;
             continue;
         }
         const PotMeta m = b.meta[w.p];
         const float2* Wf = b.Wf2 + m.offf;
         const double* W = b.W64 + m.off;
         double lo = w.lo, hi = w.hi, E = w.E, sum = 1.0;
-        int k = clamp_k(w, match_index(m, b.Msuf, E));
+        int k = mode == 2 ? w.k : grp_bcast<NW>(G, G.leader() ? clamp_k(w, match_index(m, b.Msuf, E)) : 0, sh.word);
         bool done = false;
         int n_pass = 0, n_pass32 = 0;
-        if (!fallback) {
+        if (mode == 2) {
+            // ---- stage 2 from the lane FP32 refinement (as newton_df): its sum
+            // psi~^2 is accurate to ~1e-4 on long windows, so one step is
+            // accepted from within 1e-10 and the norm pass corrects the rest
+            sum = w.norm_k_in;
+            double lo2 = w.lo - 1e-8, hi2 = w.hi + 1e-8;
+            for (int it = 0; it < 4 && !done; ++it) {
+                const PassDF r = long_pass<NW, 0>(G, m, w, Wf, W, E, k, sum, sh);
+                ++n_pass;
+                if (r.count > w.v) hi2 = fmin(hi2, E);
+                else lo2 = fmax(lo2, E);
+                const double En = E + r.dE;
+                if (!isfinite(En) || !(En >= lo2 && En <= hi2) || r.nodes != w.v) break;
+                done = fabs(r.dE) <= (it == 0 ? 1e-10 : 1e-12 * fmax(1.0, fabs(E)));
+                E = En;
+            }
+            if (done) {
+                lo = lo2;
+                hi = hi2;
+            }
+        }
+        if (mode == 0) {
             // ---- stage 1: FP32
             bool moved_last = false, ok32 = false;
             for (int it = 0, cap = refine_cap(b); it < cap; ++it) {
-                const PassDF r = long_pass32(m, w, Wf, W, E, k, sh32);
+                const PassDF r = long_pass32<NW>(G, m, w, Wf, W, E, k, sh32);
                 ++n_pass32;
                 sum = r.sum;
                 if (r.count > w.v) hi = E;
@@ -890,15 +1091,15 @@ __global__ void __launch_bounds__(kLongThreads) refine_long_kernel(DevBatch b, i
             if (ok32) {
                 double lo2 = lo - 1e-8, hi2 = hi + 1e-8;
                 for (int it = 0; it < 4 && !done; ++it) {
-                    const PassDF r = long_pass<0>(m, w, Wf, W, E, k, sum, sh);
+                    const PassDF r = long_pass<NW, 0>(G, m, w, Wf, W, E, k, sum, sh);
                     ++n_pass;
                     if (r.count > w.v) hi2 = fmin(hi2, E);
                     else lo2 = fmax(lo2, E);
                     const double En = E + r.dE;
                     if (!isfinite(En) || !(En >= lo2 && En <= hi2) || r.nodes != w.v) break;
-                    // the FP32 sum of the CTA pass is accurate to ~1e-6 (chunk
-                    // sums of a few hundred terms, added in FP64), so one step
-                    // from within 1e-8 leaves ~1e-14: the first pass settles
+                    // the FP32 sum of the group pass is accurate to ~1e-6 (chunk
+                    // sums of a few hundred terms), so one step from within 1e-8
+                    // leaves ~1e-14: the first pass settles
                     done = fabs(r.dE) <= (it == 0 ? 1e-8 * fmax(1.0, fabs(E)) : 1e-12 * fmax(1.0, fabs(E)));
                     E = En;
                 }
@@ -916,7 +1117,7 @@ __global__ void __launch_bounds__(kLongThreads) refine_long_kernel(DevBatch b, i
             if (!(E > lo && E < hi)) E = 0.5 * (lo + hi);
             bool moved_last = false;
             for (int it = 0, cap = fallback_cap(b); it < cap; ++it) {
-                const PassDF r = long_pass<1>(m, w, Wf, W, E, k, 1.0, sh);
+                const PassDF r = long_pass<NW, 1>(G, m, w, Wf, W, E, k, 1.0, sh);
                 ++n_pass;
                 sum = r.sum;
                 if (r.count > w.v) hi = E;
@@ -946,7 +1147,7 @@ __global__ void __launch_bounds__(kLongThreads) refine_long_kernel(DevBatch b, i
                 }
             }
         }
-        if (threadIdx.x == 0) {
+        if (G.leader()) {
             if (!done) w.status |= EPSCU_STATUS_MAXITER;
             w.status &= ~EPSCU_STATUS_FALLBACK;
             w.lo = lo;
@@ -958,39 +1159,38 @@ __global__ void __launch_bounds__(kLongThreads) refine_long_kernel(DevBatch b, i
             const unsigned long long pts = (unsigned long long)(w.j1 - w.j0);
             atomicAdd(&b.hdr->refine_updates, (unsigned long long)n_pass32 * pts);
             atomicAdd(&b.hdr->df_updates, (unsigned long long)n_pass * pts);
-            if (!fallback) {
+            if (mode == 0 && NW == kLongWarps) {
                 atomicAdd(&b.hdr->long32_updates, (unsigned long long)n_pass32 * pts);
                 atomicAdd(&b.hdr->longdf_updates, (unsigned long long)n_pass * pts);
             }
             b.levels[slot] = w;
         }
-        __syncthreads();
     }
 }
 
-// The norm pass of a long level and its match-point candidates (as norm_df).
-// With psi requested every pass also stores its unnormalised psi-hat in the
-// level's row (MODE 3) and the last pass is the one kept; scale_psi applies
-// the constants afterwards.
-__global__ void __launch_bounds__(kLongThreads) norm_long_kernel(DevBatch b) {
-    __shared__ LongShared sh;
-    const int n = min(b.hdr->n_long, b.max_levels);
-    __shared__ int s_q;
-    // levels from a device queue (a CTA takes the next as it finishes one)
+// The norm pass of a group level and its match-point candidates (as
+// norm_df).  With psi requested every pass also stores its unnormalised
+// psi-hat in the level's row (MODE 3) and the last pass is the one kept;
+// scale_psi applies the constants afterwards.
+template <int NW>
+__global__ void __launch_bounds__(kLongThreads) norm_long_kernel(DevBatch b, const int32_t* list,
+                                                                 const int32_t* list_len, int qid) {
+    constexpr int kG = kLongThreads / (32 * NW);
+    __shared__ SharedDF<NW> shd[kG];
+    const Grp<NW> G;
+    SharedDF<NW>& sh = shd[G.g()];
+    const int n = min(*list_len, b.max_levels);
     for (;;) {
-        if (threadIdx.x == 0) s_q = atomicAdd(&b.hdr->queue[kQNormLong], 1);
-        __syncthreads();
-        const int q = s_q;
-        __syncthreads();  // every thread has read s_q
+        const int q = grp_next<NW>(G, &b.hdr->queue[qid], sh.word);
         if (q >= n) break;
-        const int slot = b.long_list[q];
+        const int slot = list[q];
         LevelWork w = b.levels[slot];
         if (w.status & (EPSCU_STATUS_NOTFOUND | EPSCU_STATUS_CANCELLED)) continue;
         const PotMeta m = b.meta[w.p];
         const float2* Wf = b.Wf2 + m.offf;
         const double* W = b.W64 + m.off;
         double* row = psi_row(b, m, w);
-        auto pass = [&](int kk) { return long_pass<3>(m, w, Wf, W, w.E, kk, 1.0, sh, row); };
+        auto pass = [&](int kk) { return long_pass<NW, 3>(G, m, w, Wf, W, w.E, kk, 1.0, sh, row); };
         int k = w.k;
         PassDF r = pass(k);
         if (r.peak_log2 >= 2) {
@@ -999,7 +1199,7 @@ __global__ void __launch_bounds__(kLongThreads) norm_long_kernel(DevBatch b) {
         }
         int k_row = k;  // the pass whose psi-hat the row holds
         if (r.nodes != w.v) {
-            const int kt = clamp_k(w, match_index(m, b.Msuf, w.E));
+            const int kt = grp_bcast<NW>(G, G.leader() ? clamp_k(w, match_index(m, b.Msuf, w.E)) : 0, sh.word);
             PassDF r2 = pass(kt);
             int k2 = kt;
             if (r2.nodes != w.v && r2.peak_log2 >= 1) {
@@ -1013,21 +1213,20 @@ __global__ void __launch_bounds__(kLongThreads) norm_long_kernel(DevBatch b) {
             }
         }
         if (redo_norm(w, r)) {
-            if (threadIdx.x == 0) atomicAdd(&b.hdr->n_redo, 1);
+            if (G.leader()) atomicAdd(&b.hdr->n_redo, 1);
             w.E += r.dE;
             r = pass(k);
         } else if (row && k_row != k) {
             r = pass(k);
         }
-        finalize_df(m, w, r, k);
-        if (threadIdx.x == 0) {
+        if (G.leader()) {
+            finalize_df(m, w, r, k);
             if (suspicious(m, w, r.nodes, r.dE) && b.twist_list) {
                 const int t = atomicAdd(&b.hdr->n_twist, 1);
                 if (t < b.max_twist) b.twist_list[t] = slot;
             }
             b.levels[slot] = w;
         }
-        __syncthreads();
     }
 }
 
@@ -1038,17 +1237,13 @@ __global__ void __launch_bounds__(kLongThreads) norm_long_kernel(DevBatch b) {
 // rule), then Newton and the norm pass run there; with psi requested the
 // final pass stores the unnormalised psi-hat in the level's row (scale_psi
 // applies the constants).  The level joins the long list, so the adjoint's
-// recompute path (write_long) writes its psi.
+// recompute path (write_long) writes its psi.  One CTA per level.
 __global__ void __launch_bounds__(kLongThreads) twist_long_kernel(DevBatch b) {
-    __shared__ LongShared sh;
+    __shared__ SharedDF<kLongWarps> sh;
+    const Grp<kLongWarps> G;
     const int n = min(b.hdr->n_twist, b.max_twist);
-    __shared__ int s_q;
-    // levels from a device queue (a CTA takes the next as it finishes one)
     for (;;) {
-        if (threadIdx.x == 0) s_q = atomicAdd(&b.hdr->queue[kQTwistLong], 1);
-        __syncthreads();
-        const int q = s_q;
-        __syncthreads();  // every thread has read s_q
+        const int q = grp_next<kLongWarps>(G, &b.hdr->queue[kQTwistLong], sh.word);
         if (q >= n) break;
         const int slot = b.twist_list[q];
         LevelWork w = b.levels[slot];
@@ -1065,11 +1260,11 @@ __global__ void __launch_bounds__(kLongThreads) twist_long_kernel(DevBatch b) {
         tw.stride = b.twist_stride;
         tw.best = INFINITY;
         tw.k = w.k;
-        long_side<4>(Wf, aE, w.j0, w.j1, +1, nullptr, 0.0, 0, sh, &tw);
-        long_side<5>(Wf, aE, w.j1, w.j0, -1, nullptr, 0.0, 0, sh, &tw);
+        long_side<kLongWarps, 4>(G, Wf, aE, w.j0, w.j1, +1, nullptr, 0.0, 0, sh, &tw);
+        long_side<kLongWarps, 5>(G, Wf, aE, w.j1, w.j0, -1, nullptr, 0.0, 0, sh, &tw);
         const int k = clamp_k(w, tw.k == 0x7fffffff ? w.k : tw.k);
         double* row = psi_row(b, m, w);
-        auto pass = [&](double e) { return long_pass<3>(m, w, Wf, W, e, k, 1.0, sh, row); };
+        auto pass = [&](double e) { return long_pass<kLongWarps, 3>(G, m, w, Wf, W, e, k, 1.0, sh, row); };
         double E1 = w.E;
         PassDF r = pass(E1);
         for (int it = 0; it < 8; ++it) {
@@ -1079,8 +1274,8 @@ __global__ void __launch_bounds__(kLongThreads) twist_long_kernel(DevBatch b) {
             r = pass(E1);
         }
         w.E = E1;
-        finalize_df(m, w, r, k);
-        if (threadIdx.x == 0) {
+        if (G.leader()) {
+            finalize_df(m, w, r, k);
             if (!(w.status & EPSCU_STATUS_LONG) && b.long_list) {
                 const int t = atomicAdd(&b.hdr->n_long, 1);
                 if (t < b.max_levels) {
@@ -1090,18 +1285,20 @@ __global__ void __launch_bounds__(kLongThreads) twist_long_kernel(DevBatch b) {
             }
             b.levels[slot] = w;
         }
-        __syncthreads();
     }
 }
 
-// psi of the long levels in FP64 from the final constants (window points and
-// psi_k; the rest of each row is zero): the adjoint's recompute path.
-__global__ void __launch_bounds__(kLongThreads) write_long_kernel(DevBatch b) {
-    __shared__ LongShared sh;
+// psi of the listed levels in FP64 from the final constants (window points
+// and psi_k; the rest of each row is zero): the adjoint's recompute path.
+// One CTA per level.
+__global__ void __launch_bounds__(kLongThreads) write_long_kernel(DevBatch b, const int32_t* list,
+                                                                  const int32_t* list_len) {
+    __shared__ SharedDF<kLongWarps> sh;
+    const Grp<kLongWarps> G;
     if (!b.psi || b.hdr->error) return;
-    const int n = min(b.hdr->n_long, b.max_levels);
+    const int n = min(*list_len, b.max_levels);
     for (int q = blockIdx.x; q < n; q += gridDim.x) {
-        const int slot = b.long_list[q];
+        const int slot = list[q];
         const LevelWork w = b.levels[slot];
         const PotMeta m = b.meta[w.p];
         double* out = b.psi + m.psi_off + (int64_t)(w.v - b.min_level) * m.N;
@@ -1109,9 +1306,10 @@ __global__ void __launch_bounds__(kLongThreads) write_long_kernel(DevBatch b) {
         if (no_result(w)) continue;
         const float2* Wf = b.Wf2 + m.offf;
         const dfl aE = energy_df(m, w.E);
-        long_side<2>(Wf, aE, w.j0, w.k, +1, out, w.norm_k_out, w.ex_out, sh);
-        long_side<2>(Wf, aE, w.j1, w.k, -1, out, w.norm_k_in, w.ex_in, sh);
+        long_side<kLongWarps, 2>(G, Wf, aE, w.j0, w.k, +1, out, w.norm_k_out, w.ex_out, sh);
+        long_side<kLongWarps, 2>(G, Wf, aE, w.j1, w.k, -1, out, w.norm_k_in, w.ex_in, sh);
         if (threadIdx.x == 0) out[w.k] = w.ck;
+        __syncthreads();  // the shared scratch is reused by the next level
     }
 }
 
@@ -1119,23 +1317,34 @@ __global__ void __launch_bounds__(kLongThreads) write_long_kernel(DevBatch b) {
 
 void launch_refine_long(const DevBatch& b, int sm_count, cudaStream_t s) {
     if (!b.long_list) return;
-    refine_long_kernel<<<sm_count * 2, kLongThreads, 0, s>>>(b, 0);
+    refine_long_kernel<kLongWarps>
+        <<<sm_count * 2, kLongThreads, 0, s>>>(b, 0, b.long_list, &b.hdr->n_long, kQLongRefine);
 }
 void launch_fallback_long(const DevBatch& b, int sm_count, cudaStream_t s) {
     if (!b.fallback_list) return;
-    refine_long_kernel<<<sm_count * 2, kLongThreads, 0, s>>>(b, 1);
+    refine_long_kernel<kLongWarps>
+        <<<sm_count * 2, kLongThreads, 0, s>>>(b, 1, b.fallback_list, &b.hdr->fallbacks, kQFallback);
 }
 void launch_norm_long(const DevBatch& b, int sm_count, cudaStream_t s) {
     if (!b.long_list) return;
-    norm_long_kernel<<<sm_count * 2, kLongThreads, 0, s>>>(b);
+    norm_long_kernel<kLongWarps><<<sm_count * 2, kLongThreads, 0, s>>>(b, b.long_list, &b.hdr->n_long, kQNormLong);
 }
 void launch_twist_long(const DevBatch& b, int sm_count, cudaStream_t s) {
     if (!b.twist_list || !b.long_list) return;
     twist_long_kernel<<<sm_count * 2, kLongThreads, 0, s>>>(b);
 }
 void launch_write_long(const DevBatch& b, int sm_count, cudaStream_t s) {
-    if (!b.long_list) return;
-    write_long_kernel<<<sm_count * 2, kLongThreads, 0, s>>>(b);
+    // the group levels of both tiers (the recompute path: one CTA per level)
+    if (b.long_list) write_long_kernel<<<sm_count * 2, kLongThreads, 0, s>>>(b, b.long_list, &b.hdr->n_long);
+    if (b.mid_list) write_long_kernel<<<sm_count * 2, kLongThreads, 0, s>>>(b, b.mid_list, &b.hdr->n_mid);
+}
+void launch_refine_mid(const DevBatch& b, int sm_count, cudaStream_t s) {
+    if (!b.mid_list) return;
+    refine_long_kernel<1><<<sm_count * 2, kLongThreads, 0, s>>>(b, 2, b.mid_list, &b.hdr->n_mid, kQMidRefine);
+}
+void launch_norm_mid(const DevBatch& b, int sm_count, cudaStream_t s) {
+    if (!b.mid_list) return;
+    norm_long_kernel<1><<<sm_count * 2, kLongThreads, 0, s>>>(b, b.mid_list, &b.hdr->n_mid, kQNormMid);
 }
 
 }  // namespace epscu

@@ -444,7 +444,9 @@ __device__ int2 decay_window(const PotMeta& m, const DevBatch& b, double Eu, flo
 // the fallback's widened bracket), so one window serves all of them.  Levels
 // whose window is longer than the long-window threshold (DevBatch::long_window,
 // else default_long_window of the level count) go to the long list
-// (CTA-per-level passes).  One warp per level.
+// (CTA-per-level passes), those above the middle threshold to the middle list
+// (lane FP32 refinement, then warp-per-level double-float passes); the rest
+// stay on the lane kernels.  One warp per level.
 // (Sharing one window per warp unit would keep the lanes' loads of W
 // warp-wide broadcasts, but the unit's widest window costs more point-updates
 // than the divergent loads: measured slower on the mixed batch.)
@@ -454,6 +456,7 @@ __global__ void __launch_bounds__(128) window_kernel(DevBatch b, int sm_count) {
     const int total = b.hdr->total_levels;
     (void)sm_count;
     const int long_min = b.long_window > 0 ? b.long_window : default_long_window(total);
+    const int mid_min = b.mid_window < 0 || !b.mid_list ? 0x7fffffff : (b.mid_window > 0 ? b.mid_window : kMidWindow);
     for (int slot = warp; slot < total; slot += n_warps) {
         const LevelWork w = b.levels[slot];
         if (w.status & EPSCU_STATUS_NOTFOUND) continue;
@@ -467,6 +470,12 @@ __global__ void __launch_bounds__(128) window_kernel(DevBatch b, int sm_count) {
                 if (q < b.max_levels) {
                     b.long_list[q] = slot;
                     b.levels[slot].status = w.status | EPSCU_STATUS_LONG;
+                }
+            } else if (jw.y - jw.x > mid_min) {
+                const int q = atomicAdd(&b.hdr->n_mid, 1);
+                if (q < b.max_levels) {
+                    b.mid_list[q] = slot;
+                    b.levels[slot].status = w.status | EPSCU_STATUS_MID;
                 }
             }
         }

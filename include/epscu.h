@@ -93,6 +93,10 @@ typedef struct epscu_batch {
     int32_t max_level;      /* last level reported; < 0: every level below e_cap */
 } epscu_batch;
 
+/* Allocator callback: returns a device buffer of at least `bytes` bytes (16-byte
+ * aligned), or NULL when the caller cannot provide one.  See epscu_opts.psi_alloc. */
+typedef void* (*epscu_alloc_fn)(int64_t bytes, void* user);
+
 typedef struct epscu_opts {
     int32_t method;      /* EPSCU_METHOD_* */
     int32_t flags;       /* EPSCU_MEM_DEVICE | EPSCU_WANT_PSI | EPSCU_STAGE_TIMING | EPSCU_KEEP_PSI */
@@ -115,6 +119,19 @@ typedef struct epscu_opts {
     int32_t max_iter;    /* fast method: cap on the FP32 refinement passes of a level and
                             on its double-float fallback passes (0: 48 and 96); a level
                             that reaches it carries EPSCU_LEVEL_MAXITER */
+    int32_t mid_window;  /* fast method: levels whose window exceeds this many points (and
+                            not the long-window threshold) run their double-float passes one
+                            warp per level after the lane FP32 refinement (0: 1024; < 0:
+                            never, they stay one lane per level) */
+    epscu_alloc_fn psi_alloc;  /* EPSCU_MEM_DEVICE with EPSCU_WANT_PSI and result->psi NULL:
+                                  the solve reads the wavefunctions' exact size back after
+                                  its level set-up and asks psi_alloc for that buffer
+                                  (called once, from the calling thread, inside the solve);
+                                  result->psi and psi_capacity then name it.  NULL from the
+                                  callback: the solve goes on without wavefunctions
+                                  (psi_required still reports their size).  Such solves
+                                  are launched directly, not from the replayed graph. */
+    void* psi_alloc_user;      /* passed to psi_alloc */
 } epscu_opts;
 
 /* Caller-owned outputs.  Level slot s of potential p is p*level_capacity + s
