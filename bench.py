@@ -64,7 +64,8 @@ WORKLOADS = {
     "morse64": "morse_batch: 64 Morse, De~U[0.02,0.2], a~U[0.5,1.5], re~U[1.5,4], mu~logU[500,1e5], N=16384 on "
                "[0.5, re+30/a], 8192 trial energies, psi written, adjoint dL/dV",
     "adjoint256": "bump_adjoint: 256 Morse+1-3 Gaussian bumps (1024-knot spline) on N=32768, 8192 trial energies; "
-                  "loss sum_v w_v (E_v - T_v)^2, T_v = levels with bump amplitudes x1.1, w_v~U[0.5,1]",
+                  "loss sum_v w_v (E_v - T_v)^2, T_v = levels with bump amplitudes x1.1, w_v~U[0.5,1]; "
+                  "gradients to every V(r_i) and to the Morse/bump parameters",
     "long": "morse_long: one Morse (De=0.15, a=0.6, re=4, mu=1e5) on N=2^20, r in [0.5, 54], 65536 trial "
             "energies, psi written, adjoint dL/dV",
 }
@@ -325,10 +326,20 @@ def main():
     slot = torch.arange(cap, device="cuda")[None, :]
     mask = (slot < n_lev[:, None]).to(torch.float64)
 
+    # the adjoint workload differentiates to the Morse / bump parameters too
+    # (epscu_tabulate_adjoint: the spline transpose and the knot derivatives)
+    with_params = args.workload == "adjoint256"
+    if with_params:
+        P_host = capi.batch_params(b)
+        P_dev = torch.from_numpy(P_host).cuda()
+        gP_dev = torch.zeros_like(P_dev)
+
     def step():
         db.solve(capi.METHOD_FAST_FP32C, long_window=args.long_window, mid_window=args.mid_window, stream=stream.cuda_stream)
         gE = 2.0 * w * (torch.nan_to_num(db.energy) - target) * mask
         db.adjoint(gE, stream=stream.cuda_stream)
+        if with_params:
+            db.param_adjoint(b.kind, P_dev, gP_dev, stream=stream.cuda_stream)
 
     db.solve(capi.METHOD_FAST_FP32C, long_window=args.long_window, mid_window=args.mid_window, tune=True, stream=stream.cuda_stream)  # autotune the scan shape
     for _ in range(args.warmup):
@@ -385,12 +396,17 @@ def main():
                             pinned((nb, cap), torch.float64), None, pinned((nb,), torch.int64), N)
     gE_pinned = pinned((nb, cap), torch.float64)
 
+    gP_pinned = pinned((nb, 12), torch.float64) if with_params else None
+
     def e2e_step():
         sol = ctx.solve(batch_host, b.r_min, b.r_max, b.mu, b.e_cap, b.n_trial, method=capi.METHOD_FAST_FP32C,
                         level_capacity=cap, keep_psi=True, long_window=args.long_window, mid_window=args.mid_window, out=res_buf)
         np.subtract(np.nan_to_num(sol.energy), target_np, out=gE_pinned)
         np.multiply(gE_pinned, w2m, out=gE_pinned)
-        return sol, gE_pinned, ctx.adjoint(gE_pinned, Vcat.size, recompute=False, out=gV_pinned.numpy())
+        gVh = ctx.adjoint(gE_pinned, Vcat.size, recompute=False, out=gV_pinned.numpy())
+        if with_params:
+            ctx.tabulate_adjoint(b.kind, P_host, N, b.r_min, b.r_max, gVh, out=gP_pinned)
+        return sol, gE_pinned, gVh
 
     e2e_step()
     torch.cuda.synchronize()
@@ -401,6 +417,9 @@ def main():
     e2e_good, _ = count_good(b, sol.energy, sol.nodes, sol.status, ref)
     h2d = Vcat.nbytes + len(b) * (8 * 4 + 4 + 8) + gEh.nbytes
     d2h = len(b) * cap * (8 + 4 + 4 + 8) + len(b) * 8 + gVh.nbytes
+    if with_params:  # the parameter chain: params and dL/dV in, dL/dparams out
+        h2d += P_host.nbytes + gVh.nbytes + len(b) * (4 + 8 + 4 + 8 + 8)
+        d2h += gP_pinned.nbytes
 
     # ---- CPU baseline (oracle port on the host cores, bounded sample)
     cpu = None

@@ -1,17 +1,25 @@
 """torch.autograd.Function wrappers over the CUDA solver and its adjoint.
 
-This is the only place PyTorch touches the product path; the forward solve
-and the backward (Hellmann-Feynman) pass are the libepseon_cuda kernels,
-called through the C ABI on the tensors' device memory and the current
-stream.
+This is the only place PyTorch touches the product path; the forward solve,
+the backward (Hellmann-Feynman) pass and the parameter chain are
+libepseon_cuda kernels, called through the C ABI on the tensors' device
+memory and the current stream.
 
 * ``LevelEnergies`` -- V (concatenated grids, float64, cuda) -> level
   energies [n_potentials, capacity]; backward: dL/dV_i = sum_v dL/dE_v
-  psi_v(r_i)^2 h, exact for the discrete problem.
+  psi_v(r_i)^2 h, exact for the discrete problem.  The wavefunctions are
+  kept in a buffer of exactly the size the solve needs (the library reads the
+  size back after its level set-up and asks for the buffer through
+  epscu_opts.psi_alloc).  When that size is above the solver's memory budget
+  the forward keeps no wavefunctions and the backward recomputes them: it
+  re-solves the potentials in chunks whose wavefunctions fit the budget and
+  applies the adjoint chunk by chunk (the adjoint of one potential needs only
+  that potential's wavefunctions).
 * ``tabulate`` -- parameters -> V on the device (epscu_tabulate); backward is
-  the analytic derivative of the Morse / Lennard-Jones forms and, for
-  Morse+bump potentials, the transpose of the natural-cubic-spline map from
-  knots to grid (S^T) followed by the knot-level derivatives.
+  epscu_tabulate_adjoint: the analytic derivatives of the Morse and
+  Lennard-Jones forms and, for Morse+bump potentials, the transpose of the
+  natural-cubic-spline map from knots to grid (S^T) followed by the
+  knot-level derivatives, for the whole batch in one kernel.
 """
 from __future__ import annotations
 
@@ -49,45 +57,93 @@ class Grids:
     def total(self) -> int:
         return int(self.N.astype(np.int64).sum())
 
+    def subset(self, idx: np.ndarray) -> "Grids":
+        return Grids(self.N[idx].copy(), self.r_min[idx].copy(), self.r_max[idx].copy(), self.mu[idx].copy(),
+                     self.e_cap[idx].copy(), self.n_trial, self.capacity, self.method)
+
+
+def _ptr(t, ty):
+    return C.cast(C.c_void_p(t.data_ptr()), ty)
+
 
 class Solver:
-    """Owns an epscu context and the device outputs of the last solve."""
+    """Owns an epscu context and the wavefunction buffers of its solves.
 
-    def __init__(self, device: int | None = None):
+    psi_budget_bytes: the most device memory one solve's wavefunctions may
+    take (None: half of the device's free memory at the time of the solve).
+    Above it the forward keeps none and the backward recomputes them in
+    chunks that fit."""
+
+    def __init__(self, device: int | None = None, psi_budget_bytes: int | None = None):
         dev = torch.cuda.current_device() if device is None else device
         self.ctx = capi.Context(dev)
+        self.psi_budget_bytes = psi_budget_bytes
 
-    def solve(self, V: torch.Tensor, g: Grids):
-        assert V.is_cuda and V.dtype == torch.float64 and V.is_contiguous()
+    def _budget(self, dev) -> int:
+        if self.psi_budget_bytes is not None:
+            return int(self.psi_budget_bytes)
+        free, _ = torch.cuda.mem_get_info(dev)
+        return int(free) // 2
+
+    def _solve(self, V: torch.Tensor, g: Grids, budget: int):
+        """One device solve; the wavefunctions in a tensor of exactly the
+        size the solve needs, or None when that is above `budget` bytes."""
         n, cap = int(g.N.size), int(g.capacity)
         dev = V.device
-        self.n_total = torch.zeros(n, dtype=torch.int32, device=dev)
-        self.n_out = torch.zeros(n, dtype=torch.int32, device=dev)
+        n_total = torch.zeros(n, dtype=torch.int32, device=dev)
+        n_out = torch.zeros(n, dtype=torch.int32, device=dev)
         E = torch.zeros((n, cap), dtype=torch.float64, device=dev)
         nodes = torch.zeros((n, cap), dtype=torch.int32, device=dev)
         status = torch.zeros((n, cap), dtype=torch.int32, device=dev)
         err = torch.zeros((n, cap), dtype=torch.float64, device=dev)
-        psi = torch.empty(g.total * cap, dtype=torch.float64, device=dev)
         keep = [np.ascontiguousarray(x) for x in (g.offsets, g.N.astype(np.int32), g.r_min, g.r_max, g.mu, g.e_cap)]
         off, N, r0, r1, mu, ec = keep
         psi_off = np.zeros(n, np.int64)
+        held = {}
 
-        def p(t, ty):
-            return C.cast(C.c_void_p(t.data_ptr()), ty)
+        def alloc(nbytes, user):
+            if nbytes > budget:
+                return None  # too large: no wavefunctions kept
+            try:
+                t = torch.empty((int(nbytes) + 7) // 8, dtype=torch.float64, device=dev)
+            except torch.OutOfMemoryError:
+                return None
+            held["psi"] = t
+            return t.data_ptr()
 
-        b = capi.Batch(n, p(V, capi._dp), capi._l(off), capi._i(N), capi._d(r0), capi._d(r1), capi._d(mu),
+        cb = capi.ALLOC_FN(alloc)
+        b = capi.Batch(n, _ptr(V, capi._dp), capi._l(off), capi._i(N), capi._d(r0), capi._d(r1), capi._d(mu),
                        capi._d(ec), int(g.n_trial), 0, -1)
-        r = capi.Result(cap, p(self.n_total, capi._ip), p(self.n_out, capi._ip), p(E, capi._dp),
-                        p(nodes, capi._ip), p(status, capi._ip), p(err, capi._dp), p(psi, capi._dp),
-                        int(psi.numel()), capi._l(psi_off), 0)
+        r = capi.Result(cap, _ptr(n_total, capi._ip), _ptr(n_out, capi._ip), _ptr(E, capi._dp),
+                        _ptr(nodes, capi._ip), _ptr(status, capi._ip), _ptr(err, capi._dp), None, 0,
+                        capi._l(psi_off), 0)
         o = capi.Opts(int(g.method), capi.MEM_DEVICE | capi.WANT_PSI, 1e-12,
-                      C.c_void_p(torch.cuda.current_stream(dev).cuda_stream), 0, 0)
+                      C.c_void_p(torch.cuda.current_stream(dev).cuda_stream), 0, 0, 0, 0, 0, cb, None)
         capi._check(self.ctx._lib.epscu_solve(self.ctx.handle, C.byref(b), C.byref(r), C.byref(o)))
-        mask = torch.arange(cap, device=dev)[None, :] < self.n_out[:, None].long()
+        return E, nodes, status, n_out, held.get("psi"), psi_off, int(r.psi_required)
+
+    def solve(self, V: torch.Tensor, g: Grids):
+        assert V.is_cuda and V.dtype == torch.float64 and V.is_contiguous()
+        cap = int(g.capacity)
+        E, nodes, status, n_out, psi, psi_off, need = self._solve(V, g, self._budget(V.device))
+        mask = torch.arange(cap, device=V.device)[None, :] < n_out[:, None].long()
         E = torch.where(mask, E, torch.zeros_like(E))
-        # everything the adjoint of this solve needs, independent of later solves
-        self.last = SolveRecord(g, psi, psi_off.copy(), self.n_out.cpu().numpy().astype(np.int32))
+        # everything the adjoint of this solve needs, independent of later
+        # solves: the wavefunctions, or the potentials to recompute them from
+        self.last = SolveRecord(g, psi, psi_off.copy(), n_out.cpu().numpy().astype(np.int32),
+                                V if psi is None else None, need)
         return E, nodes, status, mask
+
+    def _adjoint_psi(self, g: Grids, n_out: np.ndarray, psi: torch.Tensor, psi_off: np.ndarray,
+                     gE: torch.Tensor, gV: torch.Tensor):
+        keep = [np.ascontiguousarray(x) for x in (g.offsets, g.N.astype(np.int32), g.r_min, g.r_max, n_out,
+                                                   psi_off)]
+        off, N, r0, r1, no, po = keep
+        o = capi.Opts(0, capi.MEM_DEVICE, 0.0, C.c_void_p(torch.cuda.current_stream(gE.device).cuda_stream), 0, 0)
+        capi._check(self.ctx._lib.epscu_adjoint_psi(
+            self.ctx.handle, int(N.size), capi._l(off), capi._i(N), capi._d(r0), capi._d(r1), capi._i(no),
+            int(g.capacity), _ptr(psi, capi._dp), capi._l(po), _ptr(gE, capi._dp), _ptr(gV, capi._dp),
+            C.byref(o)))
 
     def adjoint(self, gE: torch.Tensor, rec: "SolveRecord | None" = None) -> torch.Tensor:
         """dL/dV of a recorded solve (default: this solver's last one)."""
@@ -95,25 +151,47 @@ class Solver:
         g = rec.grids
         gE = gE.to(torch.float64).contiguous()
         gV = torch.zeros(g.total, dtype=torch.float64, device=gE.device)
-        keep = [np.ascontiguousarray(x) for x in (g.offsets, g.N.astype(np.int32), g.r_min, g.r_max, rec.n_out,
-                                                   rec.psi_offsets)]
-        off, N, r0, r1, no, po = keep
-        o = capi.Opts(0, capi.MEM_DEVICE, 0.0, C.c_void_p(torch.cuda.current_stream(gE.device).cuda_stream), 0, 0)
-        capi._check(self.ctx._lib.epscu_adjoint_psi(
-            self.ctx.handle, int(N.size), capi._l(off), capi._i(N), capi._d(r0), capi._d(r1), capi._i(no),
-            int(g.capacity), C.cast(C.c_void_p(rec.psi.data_ptr()), capi._dp), capi._l(po),
-            C.cast(C.c_void_p(gE.data_ptr()), capi._dp), C.cast(C.c_void_p(gV.data_ptr()), capi._dp), C.byref(o)))
+        if rec.psi is not None:
+            self._adjoint_psi(g, rec.n_out, rec.psi, rec.psi_offsets, gE, gV)
+            return gV
+        # recompute: potentials in chunks whose wavefunctions fit the budget
+        budget = self._budget(gE.device)
+        per = rec.n_out.astype(np.int64) * g.N.astype(np.int64) * 8
+        off = g.offsets
+        first = 0
+        n = int(g.N.size)
+        while first < n:
+            last, used = first, 0
+            while last < n and (last == first or used + per[last] <= budget):
+                used += int(per[last])
+                last += 1
+            idx = np.arange(first, last)
+            gc = g.subset(idx)
+            a, z = int(off[first]), int(off[last - 1] + g.N[last - 1])
+            Vc = rec.V[a:z]
+            _, _, _, n_out_c, psi_c, psi_off_c, _ = self._solve(Vc, gc, max(budget, int(per[idx].sum())))
+            n_out_c = n_out_c.cpu().numpy().astype(np.int32)
+            if psi_c is None or not np.array_equal(n_out_c, rec.n_out[idx]):
+                raise RuntimeError("wavefunction recompute failed for potentials %d..%d" % (first, last - 1))
+            gVc = torch.zeros(z - a, dtype=torch.float64, device=gE.device)
+            self._adjoint_psi(gc, n_out_c, psi_c, psi_off_c, gE[first:last].contiguous(), gVc)
+            gV[a:z] = gVc
+            del psi_c
+            first = last
         return gV
 
 
 @dataclass
 class SolveRecord:
-    """Wavefunctions and layout of one solve (kept by autograd for its backward)."""
+    """Wavefunctions and layout of one solve (kept by autograd for its
+    backward), or the potentials to recompute them from."""
 
     grids: Grids
-    psi: torch.Tensor
+    psi: torch.Tensor | None
     psi_offsets: np.ndarray
     n_out: np.ndarray
+    V: torch.Tensor | None = None
+    psi_required: int = 0  # doubles the wavefunctions take
 
 
 class LevelEnergies(torch.autograd.Function):
@@ -140,90 +218,40 @@ def levels(V: torch.Tensor, grids: Grids, solver: Solver | None = None):
 # ------------------------------------------------------------- tabulation
 
 
-def _spline_transpose_factory(n_knots: int, device):
-    """Dense inverse of the natural-spline system tridiag(1, 4, 1) (K-2)^2."""
-    m = n_knots - 2
-    A = torch.diag(torch.full((m,), 4.0, dtype=torch.float64))
-    A += torch.diag(torch.ones(m - 1, dtype=torch.float64), 1) + torch.diag(torch.ones(m - 1, dtype=torch.float64), -1)
-    return torch.linalg.inv(A).to(device)
+def _tab_args(kind: np.ndarray, grids: Grids):
+    return [np.ascontiguousarray(x) for x in (kind.astype(np.int32), grids.offsets, grids.N.astype(np.int32),
+                                               grids.r_min, grids.r_max)]
 
 
 class Tabulate(torch.autograd.Function):
-    """V = tabulate(params) on the device; analytic backward."""
+    """V = tabulate(params) on the device; backward by epscu_tabulate_adjoint."""
 
     @staticmethod
     def forward(ctx, params: torch.Tensor, kind: np.ndarray, grids: Grids, n_knots: int, solver: Solver):
         P = params.detach().to(torch.float64).contiguous()
         n = int(grids.N.size)
         V = torch.zeros(grids.total, dtype=torch.float64, device=P.device)
-        keep = [np.ascontiguousarray(x) for x in (kind.astype(np.int32), grids.offsets, grids.N.astype(np.int32),
-                                                   grids.r_min, grids.r_max)]
-        k, off, N, r0, r1 = keep
+        k, off, N, r0, r1 = _tab_args(kind, grids)
         o = capi.Opts(0, capi.MEM_DEVICE, 0.0, C.c_void_p(torch.cuda.current_stream(P.device).cuda_stream), 0, 0)
         capi._check(solver.ctx._lib.epscu_tabulate(
-            solver.ctx.handle, n, capi._i(k), C.cast(C.c_void_p(P.data_ptr()), capi._dp), capi._l(off),
-            capi._i(N), capi._d(r0), capi._d(r1), int(n_knots), C.cast(C.c_void_p(V.data_ptr()), capi._dp),
-            C.byref(o)))
+            solver.ctx.handle, n, capi._i(k), _ptr(P, capi._dp), capi._l(off), capi._i(N), capi._d(r0),
+            capi._d(r1), int(n_knots), _ptr(V, capi._dp), C.byref(o)))
         ctx.save_for_backward(P)
-        ctx.kind, ctx.grids, ctx.n_knots = kind, grids, n_knots
+        ctx.kind, ctx.grids, ctx.n_knots, ctx.solver = kind, grids, n_knots, solver
         return V
 
     @staticmethod
     def backward(ctx, gV):
         (P,) = ctx.saved_tensors
-        grids, kind, K = ctx.grids, ctx.kind, ctx.n_knots
-        dev = P.device
+        grids = ctx.grids
+        n = int(grids.N.size)
+        gV = gV.to(torch.float64).contiguous()
         gP = torch.zeros_like(P)
-        off = grids.offsets
-        Ainv = None
-        for p in range(int(grids.N.size)):
-            Np = int(grids.N[p])
-            g = gV[int(off[p]): int(off[p]) + Np]
-            r = grids.r_min[p] + torch.arange(Np, dtype=torch.float64, device=dev) * (
-                (grids.r_max[p] - grids.r_min[p]) / (Np - 1))
-            if int(kind[p]) == KIND_LJ:
-                eps, sig = P[p, 0], P[p, 1]
-                s6 = (sig / r) ** 6
-                gP[p, 0] = torch.sum(g * (4.0 * (s6 * s6 - s6) + 1.0))
-                gP[p, 1] = torch.sum(g * 4.0 * eps * (12.0 * s6 * s6 - 6.0 * s6) / sig)
-                continue
-            if int(kind[p]) == KIND_MORSE:
-                gy, rk = g, r
-            else:
-                # g at the knots: S^T g for the natural cubic spline on K uniform knots
-                if Ainv is None:
-                    Ainv = _spline_transpose_factory(K, dev)
-                hk = (grids.r_max[p] - grids.r_min[p]) / (K - 1)
-                t = (r - grids.r_min[p]) / hk
-                j = torch.clamp(torch.floor(t).long(), 0, K - 2)
-                u = t - j
-                w = 1.0 - u
-                gy = torch.zeros(K, dtype=torch.float64, device=dev)
-                gy.index_add_(0, j, g * w)
-                gy.index_add_(0, j + 1, g * u)
-                gM = torch.zeros(K, dtype=torch.float64, device=dev)
-                h2 = hk * hk / 6.0
-                gM.index_add_(0, j, g * h2 * (w ** 3 - w))
-                gM.index_add_(0, j + 1, g * h2 * (u ** 3 - u))
-                # M_int = Ainv @ (6/hk^2) D2 y  ->  gy += D2^T (6/hk^2) Ainv^T gM_int
-                z = Ainv.T @ gM[1:-1] * (6.0 / (hk * hk))
-                gy[:-2] += z
-                gy[1:-1] -= 2.0 * z
-                gy[2:] += z
-                rk = grids.r_min[p] + torch.arange(K, dtype=torch.float64, device=dev) * hk
-            De, a, re = P[p, 0], P[p, 1], P[p, 2]
-            ex = torch.exp(-a * (rk - re))
-            x = 1.0 - ex
-            gP[p, 0] = torch.sum(gy * x * x)
-            gP[p, 1] = torch.sum(gy * 2.0 * De * x * ex * (rk - re))
-            gP[p, 2] = torch.sum(gy * -2.0 * De * x * ex * a)
-            if int(kind[p]) == KIND_SPLINE:
-                for q in range(3):
-                    amp, wd, c = P[p, 3 + 3 * q], P[p, 4 + 3 * q], P[p, 5 + 3 * q]
-                    gauss = torch.exp(-((rk - c) ** 2) / (2.0 * wd * wd))
-                    gP[p, 3 + 3 * q] = torch.sum(gy * gauss)
-                    gP[p, 4 + 3 * q] = torch.sum(gy * amp * gauss * (rk - c) ** 2 / wd ** 3)
-                    gP[p, 5 + 3 * q] = torch.sum(gy * amp * gauss * (rk - c) / (wd * wd))
+        k, off, N, r0, r1 = _tab_args(ctx.kind, grids)
+        o = capi.Opts(0, capi.MEM_DEVICE, 0.0, C.c_void_p(torch.cuda.current_stream(P.device).cuda_stream), 0, 0)
+        capi._check(ctx.solver.ctx._lib.epscu_tabulate_adjoint(
+            ctx.solver.ctx.handle, n, capi._i(k), _ptr(P, capi._dp), capi._l(off), capi._i(N), capi._d(r0),
+            capi._d(r1), int(ctx.n_knots), _ptr(gV, capi._dp), _ptr(gP, capi._dp), C.byref(o)))
         return gP, None, None, None, None
 
 

@@ -145,6 +145,7 @@ EXPORTED = [
     "epscu_adjoint",
     "epscu_adjoint_psi",
     "epscu_tabulate",
+    "epscu_tabulate_adjoint",
     "epscu_cancel",
     "epscu_cancel_clear",
     "epscu_last_stats",
@@ -187,6 +188,8 @@ def load(build_if_missing: bool = True):
     L.epscu_adjoint_psi.argtypes = [C.c_void_p, C.c_int32, _lp, _ip, _dp, _dp, _ip, C.c_int32, _dp, _lp, _dp, _dp,
                                     C.POINTER(Opts)]
     L.epscu_tabulate.argtypes = [C.c_void_p, C.c_int32, _ip, _dp, _lp, _ip, _dp, _dp, C.c_int32, _dp, C.POINTER(Opts)]
+    L.epscu_tabulate_adjoint.argtypes = [C.c_void_p, C.c_int32, _ip, _dp, _lp, _ip, _dp, _dp, C.c_int32, _dp, _dp,
+                                         C.POINTER(Opts)]
     L.epscu_cancel.argtypes = [C.c_void_p]
     L.epscu_cancel_clear.argtypes = [C.c_void_p]
     L.epscu_last_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
@@ -418,6 +421,24 @@ class Context:
         _check(self._lib.epscu_adjoint(self._h, _d(g), _d(out), 1 if recompute else 0, C.byref(o)))
         return out
 
+    def tabulate_adjoint(self, kind, params, N, r_min, r_max, dL_dV, n_knots: int = 1024,
+                         out: np.ndarray | None = None) -> np.ndarray:
+        """dL/dparams [n, 12] from dL/dV (host arrays; epscu_tabulate_adjoint)."""
+        kind = np.ascontiguousarray(kind, np.int32)
+        params = np.ascontiguousarray(params, np.float64).reshape(-1, 12)
+        N = np.ascontiguousarray(N, np.int32)
+        offsets = np.zeros(N.size, np.int64)
+        offsets[1:] = np.cumsum(N[:-1].astype(np.int64))
+        r_min = np.ascontiguousarray(r_min, np.float64)
+        r_max = np.ascontiguousarray(r_max, np.float64)
+        g = np.ascontiguousarray(dL_dV, np.float64)
+        if out is None:
+            out = np.zeros((N.size, 12))
+        o = Opts(0, 0, 0.0, None, 0, 0)
+        _check(self._lib.epscu_tabulate_adjoint(self._h, int(N.size), _i(kind), _d(params), _l(offsets), _i(N),
+                                                _d(r_min), _d(r_max), int(n_knots), _d(g), _d(out), C.byref(o)))
+        return out
+
     def tabulate(self, kind, params, N, r_min, r_max, n_knots: int = 1024) -> list:
         kind = np.ascontiguousarray(kind, np.int32)
         params = np.ascontiguousarray(params, np.float64).reshape(-1, 12)
@@ -511,6 +532,21 @@ class DeviceBatch:
         o = Opts(int(method), flags, 1e-12, C.c_void_p(s), 1 if tune else 0, int(long_window), 0, 0, int(mid_window))
         _check(self.ctx._lib.epscu_solve(self.ctx.handle, C.byref(b), C.byref(r), C.byref(o)))
         self.psi_required = r.psi_required
+
+    def param_adjoint(self, kind, params, gP=None, n_knots: int = 1024, stream=None):
+        """dL/dparams [n, 12] (device) from self.gV through epscu_tabulate_adjoint;
+        params: the [n, 12] float64 cuda tensor the potentials were tabulated from."""
+        import torch
+
+        kind = np.ascontiguousarray(kind, np.int32)
+        if gP is None:
+            gP = torch.zeros((self.n, 12), dtype=torch.float64, device=self.gV.device)
+        s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        o = Opts(0, MEM_DEVICE, 0.0, C.c_void_p(s), 0, 0)
+        _check(self.ctx._lib.epscu_tabulate_adjoint(
+            self.ctx.handle, self.n, _i(kind), self._ptr(params, _dp), _l(self.offsets), _i(self.N),
+            _d(self.r_min), _d(self.r_max), int(n_knots), self._ptr(self.gV, _dp), self._ptr(gP, _dp), C.byref(o)))
+        return gP
 
     def adjoint(self, gE, recompute: bool = False, stream=None):
         """dL/dV into self.gV (device) for dL/dE = gE ([n, cap] float64 cuda tensor)."""

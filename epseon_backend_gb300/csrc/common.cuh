@@ -75,6 +75,8 @@ struct Header {
     int32_t n_long;         // levels whose window takes the CTA-per-level passes
     int32_t n_mid;          // levels whose window takes the warp-per-level passes
     int32_t pad_mid;
+    int32_t bis_items_n;    // bisection round: (potential, chunk) items listed
+    int32_t bis_items_q;    //   and the work-queue head over them
     int32_t n_redo;         // norm passes redone at E + dE
     unsigned long long scan_updates;    // point-updates the windowed FP32 scan performed
     unsigned long long refine_updates;  // point-updates of the FP32 refinement passes

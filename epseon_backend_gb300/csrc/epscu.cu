@@ -481,6 +481,8 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     b.mid_list = nullptr;
     b.bis_list = nullptr;
     b.bis_n = nullptr;
+    b.bis_items = nullptr;
+    b.max_bis_items = 0;
     b.Mpre = nullptr;
     b.Bmin = nullptr;
     if (method == EPSCU_METHOD_FAST_FP32C) {
@@ -498,7 +500,10 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
             // batches: the bisection scan (counts where they change only)
             b.bis_list = (int32_t*)ctx->get("bis_list", sizeof(int32_t) * (size_t)n * batch->n_trial, &ce);
             b.bis_n = (int32_t*)ctx->get("bis_n", sizeof(int32_t) * (size_t)n, &ce);
-            if (!b.bis_list || !b.bis_n) return fail(EPSCU_ERR_NOMEM, "device arena (bisection scan)");
+            const int64_t items = bisect_max_items(n, batch->n_trial);
+            b.bis_items = (int2*)ctx->get("bis_items", sizeof(int2) * (size_t)items, &ce);
+            b.max_bis_items = (int32_t)std::min<int64_t>(items, 1 << 30);
+            if (!b.bis_list || !b.bis_n || !b.bis_items) return fail(EPSCU_ERR_NOMEM, "device arena (bisection scan)");
         }
     }
     int64_t* d_off = (int64_t*)ctx->get("offsets", sizeof(int64_t) * n, &ce);
@@ -966,6 +971,64 @@ extern "C" epscu_status epscu_tabulate(epscu_ctx* ctx, int32_t n, const int32_t*
     launch_tabulate(n, d_kind, d_par, d_off, d_N, d_r0, d_r1, n_knots, d_scr, out, s);
     EPSCU_CU(cudaGetLastError());
     if (!dev) EPSCU_CU(cudaMemcpyAsync(V, out, sizeof(double) * total, cudaMemcpyDeviceToHost, s));
+    EPSCU_CU(cudaEventRecord(ctx->ev_out, s));
+    EPSCU_CU(cudaStreamWaitEvent(caller, ctx->ev_out, 0));
+    EPSCU_CU(cudaStreamSynchronize(s));
+    return EPSCU_OK;
+}
+
+extern "C" epscu_status epscu_tabulate_adjoint(epscu_ctx* ctx, int32_t n, const int32_t* kind, const double* params,
+                                               const int64_t* offsets, const int32_t* N, const double* r_min,
+                                               const double* r_max, int32_t n_knots, const double* dL_dV,
+                                               double* dL_dparams, const epscu_opts* opts_in) {
+    if (!ctx || n <= 0 || !kind || !params || !offsets || !N || !r_min || !r_max || !dL_dV || !dL_dparams)
+        return fail(EPSCU_ERR_INVALID, "bad arguments");
+    if (n_knots < 4) n_knots = 1024;
+    epscu_opts opts{};
+    if (opts_in) opts = *opts_in;
+    std::lock_guard<std::mutex> guard(ctx->mu);
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = ctx->stream;
+    const cudaStream_t caller = caller_stream(opts);
+    EPSCU_CU(cudaEventRecord(ctx->ev_in, caller));
+    EPSCU_CU(cudaStreamWaitEvent(s, ctx->ev_in, 0));
+    const bool dev = (opts.flags & EPSCU_MEM_DEVICE) != 0;
+    int64_t total = 0;
+    for (int p = 0; p < n; ++p) {
+        if (N[p] < 2) return fail(EPSCU_ERR_INVALID, "grid with fewer than 2 points");
+        if (kind[p] < EPSCU_KIND_MORSE || kind[p] > EPSCU_KIND_SPLINE) return fail(EPSCU_ERR_INVALID, "unknown kind");
+        total = std::max<int64_t>(total, offsets[p] + N[p]);
+    }
+    cudaError_t ce = cudaSuccess;
+    auto* d_kind = (int32_t*)ctx->get("tab_kind", sizeof(int32_t) * n, &ce);
+    auto* d_off = (int64_t*)ctx->get("tab_off", sizeof(int64_t) * n, &ce);
+    auto* d_N = (int32_t*)ctx->get("tab_N", sizeof(int32_t) * n, &ce);
+    auto* d_r0 = (double*)ctx->get("tab_r0", sizeof(double) * n, &ce);
+    auto* d_r1 = (double*)ctx->get("tab_r1", sizeof(double) * n, &ce);
+    auto* d_scr = (double*)ctx->get("tabadj_scratch", sizeof(double) * 6 * (size_t)n_knots * n, &ce);
+    if (!d_kind || !d_off || !d_N || !d_r0 || !d_r1 || !d_scr) return fail(EPSCU_ERR_NOMEM, "device arena");
+    EPSCU_CU(cudaMemcpyAsync(d_kind, kind, sizeof(int32_t) * n, cudaMemcpyHostToDevice, s));
+    EPSCU_CU(cudaMemcpyAsync(d_off, offsets, sizeof(int64_t) * n, cudaMemcpyHostToDevice, s));
+    EPSCU_CU(cudaMemcpyAsync(d_N, N, sizeof(int32_t) * n, cudaMemcpyHostToDevice, s));
+    EPSCU_CU(cudaMemcpyAsync(d_r0, r_min, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    EPSCU_CU(cudaMemcpyAsync(d_r1, r_max, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    const double* d_par = params;
+    const double* d_gV = dL_dV;
+    double* d_gP = dL_dparams;
+    if (!dev) {
+        auto* a = (double*)ctx->get("tabadj_par", sizeof(double) * 12 * n, &ce);
+        auto* b = (double*)ctx->get("tabadj_gV", sizeof(double) * total, &ce);
+        auto* c = (double*)ctx->get("tabadj_gP", sizeof(double) * 12 * n, &ce);
+        if (!a || !b || !c) return fail(EPSCU_ERR_NOMEM, "device arena");
+        EPSCU_CU(cudaMemcpyAsync(a, params, sizeof(double) * 12 * n, cudaMemcpyHostToDevice, s));
+        EPSCU_CU(cudaMemcpyAsync(b, dL_dV, sizeof(double) * total, cudaMemcpyHostToDevice, s));
+        d_par = a;
+        d_gV = b;
+        d_gP = c;
+    }
+    launch_tabulate_adjoint(n, d_kind, d_par, d_off, d_N, d_r0, d_r1, n_knots, d_scr, d_gV, d_gP, s);
+    EPSCU_CU(cudaGetLastError());
+    if (!dev) EPSCU_CU(cudaMemcpyAsync(dL_dparams, d_gP, sizeof(double) * 12 * n, cudaMemcpyDeviceToHost, s));
     EPSCU_CU(cudaEventRecord(ctx->ev_out, s));
     EPSCU_CU(cudaStreamWaitEvent(caller, ctx->ev_out, 0));
     EPSCU_CU(cudaStreamSynchronize(s));

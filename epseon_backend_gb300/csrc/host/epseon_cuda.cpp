@@ -423,6 +423,28 @@ void TaskHandle<FP>::execute(std::stop_token st) {
     const size_t total = src.size();
     const size_t group = hw.group_size ? hw.group_size : total;
     const int32_t cap = (int32_t)(alg.max_level - alg.min_level + 1);
+    const double dist = to_hartree(alg.min_distance_to_asymptote);
+    // the widest energy window of a group's potentials (cap - min V)
+    auto span_of = [&](const PotentialBatchData& d) {
+        double span = 0.0;
+        for (size_t i = 0; i < d.N.size(); ++i) {
+            const int64_t o = d.offsets[i];
+            double vmin = d.V[o];
+            for (int32_t j = 0; j < d.N[i]; ++j) vmin = std::min(vmin, d.V[o + j]);
+            span = std::max(span, d.asymptote[i] - dist - vmin);
+        }
+        return span;
+    };
+    // The trial grid is the task's, not the group's: n_trial follows the
+    // widest window of the whole task, so splitting a task into groups
+    // (HardwareConfig::group_size) changes no result.  With several groups
+    // the potentials are tabulated once more for this.
+    double task_span = -1.0;
+    if (group < total) {
+        task_span = 0.0;
+        for (size_t first = 0; first < total && !st.stop_requested(); first += group)
+            task_span = std::max(task_span, span_of(src.get_potential_data(ctx, first, std::min(group, total - first))));
+    }
     res = TaskResults{};
     for (size_t first = 0; first < total; first += group) {
         if (st.stop_requested()) {
@@ -434,14 +456,8 @@ void TaskHandle<FP>::execute(std::stop_token st) {
         PotentialBatchData d = src.get_potential_data(ctx, first, count);
         const int n = (int)count;
         std::vector<double> mus(n, mu), cap_e(n);
-        double max_span = 0.0;
-        for (int i = 0; i < n; ++i) {
-            const int64_t o = d.offsets[i];
-            double vmin = d.V[o];
-            for (int32_t j = 0; j < d.N[i]; ++j) vmin = std::min(vmin, d.V[o + j]);
-            cap_e[i] = d.asymptote[i] - to_hartree(alg.min_distance_to_asymptote);
-            max_span = std::max(max_span, cap_e[i] - vmin);
-        }
+        for (int i = 0; i < n; ++i) cap_e[i] = d.asymptote[i] - dist;
+        const double max_span = task_span >= 0.0 ? task_span : span_of(d);
         int32_t n_trial = 1024;
         if (alg.integration_step > 0) {
             const double want = std::ceil(max_span / to_hartree(alg.integration_step));

@@ -38,6 +38,8 @@ struct DevBatch {
     int32_t* bis_list;         // [n * n_trial] trial indices of the bisection scan's current round, or
                                // nullptr (every trial energy scanned)
     int32_t* bis_n;            // [n] entries of bis_list per potential
+    int2* bis_items;           // [max_bis_items] (potential, first entry) chunks of a bisection round
+    int32_t max_bis_items;
     double* psi;               // compact wavefunctions or nullptr
     int64_t psi_capacity;
     volatile int32_t* cancel;  // host-mapped cancel flag (device pointer) or nullptr
@@ -83,6 +85,10 @@ void launch_tabulate(int32_t n, const int32_t* kind, const double* params, const
                      const int32_t* N, const double* r_min, const double* r_max, int32_t n_knots,
                      double* knot_scratch, double* V, cudaStream_t s);
 
+void launch_tabulate_adjoint(int32_t n, const int32_t* kind, const double* params, const int64_t* offsets,
+                             const int32_t* N, const double* r_min, const double* r_max, int32_t n_knots,
+                             double* knot_scratch, const double* gV, double* gP, cudaStream_t s);
+
 // scan.cu
 void launch_scan64(const DevBatch& b, cudaStream_t s);
 struct ScanShape {
@@ -93,6 +99,7 @@ struct ScanShape {
 };
 void launch_scan32(const DevBatch& b, const ScanShape& shape, int sm_count, cudaStream_t s, int stride = 1);
 void launch_bisect_scan(const DevBatch& b, const ScanShape& shape, int sm_count, cudaStream_t s);
+int64_t bisect_max_items(int n, int n_trial);  // capacity of DevBatch::bis_items
 int scan32_max_tile();
 void scan32_set_attributes();
 

@@ -575,7 +575,170 @@ __global__ void tabulate_kernel(int32_t n, const int32_t* kind, const double* pa
     }
 }
 
+// The adjoint of tabulate_kernel: dL/dparams from dL/dV, one CTA per
+// potential (kTabAdjThreads threads), in FP64.
+//   Morse, LJ: sum_i g_i dV_i/dtheta over the grid.
+//   Morse + bumps through the spline: V_i = w y_j + u y_{j+1}
+//     + hk^2/6 ((w^3 - w) M_j + (u^3 - u) M_{j+1}) with M = A^-1 (6/hk^2) D2 y
+//     (A = tridiag(1, 4, 1) on the interior knots, M_0 = M_{K-1} = 0), so
+//     dL/dy = S^T g = P^T g + (6/hk^2) D2^T A^-1 Q^T g, with P^T g and Q^T g
+//     the grid's pull-back onto the knots (the w/u and the cubic weights) and
+//     A^-1 applied by the same Thomas sweep as the forward; then
+//     sum_k dL/dy_k dy_k/dtheta over the knots (Morse and Gaussian terms).
+// The pull-back is deterministic: each thread owns a contiguous range of knot
+// intervals and the grid points that fall in them (the same interval rule as
+// the forward), writing the interval's left and right sums; every sum then
+// runs in a fixed order (no atomics), so repeated calls give identical bits.
+constexpr int kTabAdjThreads = 256;
+
+__device__ __forceinline__ int tab_interval(int i, double r0, double h, double hk, int n_knots) {
+    const double r = r0 + i * h;
+    const double t = (r - r0) / hk;
+    int j = (int)floor(t);
+    return max(0, min(j, n_knots - 2));
+}
+
+// deterministic sum of one value per thread over the CTA (fixed tree)
+__device__ __forceinline__ double cta_sum(double v, double* red) {
+    red[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = kTabAdjThreads / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    const double r = red[0];
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(kTabAdjThreads) tabulate_adjoint_kernel(
+    int32_t n, const int32_t* kind, const double* params, const int64_t* offsets, const int32_t* Ns,
+    const double* r_min, const double* r_max, int32_t n_knots, double* scratch, const double* gV, double* gP) {
+    __shared__ double red[kTabAdjThreads];
+    const int p = blockIdx.x;
+    const int N = Ns[p];
+    const double r0 = r_min[p], r1 = r_max[p];
+    const double h = (r1 - r0) / (double)(N - 1);
+    const double* P = params + (int64_t)p * 12;
+    const double* g = gV + offsets[p];
+    double acc[12];
+    for (int q = 0; q < 12; ++q) acc[q] = 0.0;
+    const int k = kind[p];
+    if (k == EPSCU_KIND_SPLINE) {
+        const int K = n_knots;
+        const double hk = (r1 - r0) / (double)(K - 1);
+        const double h2 = hk * hk / 6.0, s6 = 6.0 / (hk * hk);
+        double* Ly = scratch + (int64_t)p * 6 * K;  // per interval: left and right sums of w, u weights
+        double* Ry = Ly + K;
+        double* LM = Ry + K;                          // and of the cubic weights
+        double* RM = LM + K;
+        double* z = RM + K;                           // A^-1 (Q^T g) on the interior knots
+        double* cp = z + K;
+        // ---- pull-back onto the knot intervals [jb, je) owned by this thread
+        const int nint = K - 1;
+        const int per = (nint + kTabAdjThreads - 1) / kTabAdjThreads;
+        const int jb = min((int)threadIdx.x * per, nint), je = min(jb + per, nint);
+        if (jb < je) {
+            // first grid point of interval jb: an estimate, then the forward's rule
+            int i = (int)fmax(0.0, floor(jb * hk / h) - 2.0);
+            i = min(i, N - 1);
+            while (i > 0 && tab_interval(i, r0, h, hk, K) >= jb) --i;
+            while (i < N && tab_interval(i, r0, h, hk, K) < jb) ++i;
+            for (int j = jb; j < je; ++j) {
+                double ly = 0.0, ry = 0.0, lm = 0.0, rm = 0.0;
+                for (; i < N; ++i) {
+                    const double r = r0 + i * h;
+                    const double t = (r - r0) / hk;
+                    int jj = (int)floor(t);
+                    jj = max(0, min(jj, K - 2));
+                    if (jj != j) break;
+                    const double u = t - jj, w = 1.0 - u;
+                    const double gi = g[i];
+                    ly += gi * w;
+                    ry += gi * u;
+                    lm += gi * h2 * (w * w * w - w);
+                    rm += gi * h2 * (u * u * u - u);
+                }
+                Ly[j] = ly;
+                Ry[j] = ry;
+                LM[j] = lm;
+                RM[j] = rm;
+            }
+        }
+        __syncthreads();
+        // ---- z = A^-1 (Q^T g)_interior (A symmetric): the forward's Thomas sweep
+        if (threadIdx.x == 0) {
+            const int nn = K - 2;
+            auto gm = [&](int kk) { return LM[kk] + (kk > 0 ? RM[kk - 1] : 0.0); };  // (Q^T g) at knot kk
+            cp[0] = 1.0 / 4.0;
+            z[1] = gm(1) / 4.0;
+            for (int q = 1; q < nn; ++q) {
+                const double den = 4.0 - cp[q - 1];
+                cp[q] = 1.0 / den;
+                z[q + 1] = (gm(q + 1) - z[q]) / den;
+            }
+            for (int q = nn - 2; q >= 0; --q) z[q + 1] = z[q + 1] - cp[q] * z[q + 2];
+            z[0] = 0.0;
+            z[K - 1] = 0.0;
+        }
+        __syncthreads();
+        // ---- dL/dy_k = (P^T g)_k + s6 (D2^T z)_k, then the knots' parameter derivatives
+        for (int kk = threadIdx.x; kk < K; kk += kTabAdjThreads) {
+            double gy = Ly[kk] + (kk > 0 ? Ry[kk - 1] : 0.0);
+            const double zl = kk >= 1 ? z[kk - 1] : 0.0, zc = z[kk], zr = kk + 1 < K ? z[kk + 1] : 0.0;
+            gy += s6 * (zl - 2.0 * zc + zr);
+            const double r = r0 + kk * hk;
+            const double De = P[0], a = P[1], re = P[2];
+            const double e = exp(-a * (r - re));
+            const double x = 1.0 - e;
+            acc[0] += gy * x * x;
+            acc[1] += gy * 2.0 * De * x * e * (r - re);
+            acc[2] += gy * -2.0 * De * x * e * a;
+            for (int q = 0; q < 3; ++q) {
+                const double amp = P[3 + 3 * q], wd = P[4 + 3 * q], c = P[5 + 3 * q];
+                if (amp == 0.0) continue;
+                const double d = r - c;
+                const double G = exp(-(d * d) / (2.0 * wd * wd));
+                acc[3 + 3 * q] += gy * G;
+                acc[4 + 3 * q] += gy * amp * G * d * d / (wd * wd * wd);
+                acc[5 + 3 * q] += gy * amp * G * d / (wd * wd);
+            }
+        }
+    } else if (k == EPSCU_KIND_LJ) {
+        const double eps = P[0], sigma = P[1];
+        for (int i = threadIdx.x; i < N; i += kTabAdjThreads) {
+            const double r = r0 + i * h;
+            const double s = sigma / r;
+            const double s2 = s * s;
+            const double s6 = s2 * s2 * s2;
+            acc[0] += g[i] * (4.0 * (s6 * s6 - s6) + 1.0);
+            acc[1] += g[i] * 4.0 * eps * (12.0 * s6 * s6 - 6.0 * s6) / sigma;
+        }
+    } else {
+        const double De = P[0], a = P[1], re = P[2];
+        for (int i = threadIdx.x; i < N; i += kTabAdjThreads) {
+            const double r = r0 + i * h;
+            const double e = exp(-a * (r - re));
+            const double x = 1.0 - e;
+            acc[0] += g[i] * x * x;
+            acc[1] += g[i] * 2.0 * De * x * e * (r - re);
+            acc[2] += g[i] * -2.0 * De * x * e * a;
+        }
+    }
+    for (int q = 0; q < 12; ++q) {
+        const double v = cta_sum(acc[q], red);
+        if (threadIdx.x == 0) gP[(int64_t)p * 12 + q] = v;
+    }
+}
+
 }  // namespace
+
+void launch_tabulate_adjoint(int32_t n, const int32_t* kind, const double* params, const int64_t* offsets,
+                             const int32_t* N, const double* r_min, const double* r_max, int32_t n_knots,
+                             double* knot_scratch, const double* gV, double* gP, cudaStream_t s) {
+    tabulate_adjoint_kernel<<<n, kTabAdjThreads, 0, s>>>(n, kind, params, offsets, N, r_min, r_max, n_knots,
+                                                         knot_scratch, gV, gP);
+}
 
 void launch_prepare(const DevBatch& b, cudaStream_t s) {
     prepare_kernel<<<b.n, kPrepThreads, 0, s>>>(b);

@@ -428,11 +428,16 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
 // potential instead of n_trial.  counts[] holds -1 where no count was taken.
 
 // The trial indices of the next round (W = 0: the coarse boundaries; else
-// the midpoints of the cells of width W whose end counts differ).  One CTA
-// per potential.
+// the midpoints of the cells of width W whose end counts differ), and the
+// round's work items: the potential's list in chunks of kCountEnergies, so
+// that the count kernel runs every chunk of every potential side by side.
+// One CTA per potential, longest grids first (their items are listed first).
+constexpr int kCountThreads = 128;
+constexpr int kCountEnergies = kCountThreads / 2;
+
 __global__ void __launch_bounds__(256) bisect_plan_kernel(DevBatch b, int W) {
     __shared__ int s_n;
-    const int p = blockIdx.x;
+    const int p = b.order[blockIdx.x];
     const PotMeta m = b.meta[p];
     if (threadIdx.x == 0) s_n = 0;
     __syncthreads();
@@ -455,18 +460,26 @@ __global__ void __launch_bounds__(256) bisect_plan_kernel(DevBatch b, int W) {
         }
     }
     __syncthreads();
-    if (threadIdx.x == 0) b.bis_n[p] = s_n;
+    if (threadIdx.x == 0) {
+        b.bis_n[p] = s_n;
+        const int nch = (s_n + kCountEnergies - 1) / kCountEnergies;
+        if (nch > 0) {
+            const int base = atomicAdd(&b.hdr->bis_items_n, nch);
+            for (int c = 0; c < nch && base + c < b.max_bis_items; ++c)
+                b.bis_items[base + c] = make_int2(p, c * kCountEnergies);
+        }
+    }
 }
 
-// Counts at the listed trial energies of each potential: one CTA per
-// potential (longest grids first), up to kCountThreads energies at a time,
-// each thread one energy through the FP32 difference form with
-// T = (aE_hi - W_hi) + (aE_lo - W_lo) (three FADDs: the energies of a round
-// spread over the whole spectrum, so no shared reference energy), on tiles
-// of the window of the chunk's highest energy staged in shared memory.
-constexpr int kCountThreads = 128;
+// Counts at the listed trial energies: persistent CTAs take the round's
+// (potential, chunk of kCountEnergies entries) items from a device queue, so
+// a round lasts about one serial march of its longest window however many
+// levels a potential has.  Each energy is carried through the FP32
+// difference form with T = (aE_hi - W_hi) + (aE_lo - W_lo) (three FADDs: the
+// energies of a round spread over the whole spectrum, so no shared reference
+// energy), on tiles of the window of the chunk's highest energy staged in
+// shared memory.
 constexpr int kCountTile = 2048;
-constexpr int kCountSplit = 4;  // CTAs per potential (chunks of energies in parallel)
 
 // the three-FADD step on a raw (w.x, w.y) tile: per point, with the node
 // count; and with the sign history (16-step chunks, popcounted)
@@ -531,28 +544,33 @@ __device__ __forceinline__ void run_down_raw(const float2* __restrict__ tb, int 
 
 // Two threads per listed energy: warps 0-1 march the outward side, warps 2-3
 // the inward side of the same kCountEnergies energies, on their own tiles,
-// so a round waits for half of the longest window's serial march; the inward
-// half hands its state to the outward one for the twist pivot.
-constexpr int kCountEnergies = kCountThreads / 2;
-
+// so a chunk waits for half of its window's serial march; the inward half
+// hands its state to the outward one for the twist pivot.
 __global__ void __launch_bounds__(kCountThreads) count_list_kernel(DevBatch b) {
     __shared__ __align__(16) float2 tile_o[kCountTile];
     __shared__ __align__(16) float2 tile_i[kCountTile];
     __shared__ float s_A[kCountEnergies], s_D[kCountEnergies];
     __shared__ int s_nodes[kCountEnergies];
     __shared__ int s_jmax;
+    __shared__ int s_item;
     const int tid = threadIdx.x;
     const int side = tid / kCountEnergies;  // 0: outward, 1: inward (warp-uniform)
     const int e = tid - side * kCountEnergies;
-    const int p = b.order[blockIdx.x];
-    const PotMeta m = b.meta[p];
-    const int ne = b.bis_n[p];
-    if (ne <= 0 || (m.status & EPSCU_STATUS_BAD)) return;
-    const int32_t* list = b.bis_list + (int64_t)p * b.n_trial;
-    const float2* src = b.Wf2 + m.offf;  // padded to whole tiles
-    const int k = m.k_scan;
-    // chunks of kCountEnergies energies, spread over gridDim.y CTAs
-    for (int c0 = blockIdx.y * kCountEnergies; c0 < ne; c0 += gridDim.y * kCountEnergies) {
+    const int n_items = min(b.hdr->bis_items_n, b.max_bis_items);
+    for (;;) {
+        __syncthreads();  // everyone has read the previous item
+        if (tid == 0) s_item = atomicAdd(&b.hdr->bis_items_q, 1);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= n_items) break;
+        const int2 it = b.bis_items[item];
+        const int p = it.x, c0 = it.y;
+        const PotMeta m = b.meta[p];
+        const int ne = b.bis_n[p];
+        if (ne <= 0 || (m.status & EPSCU_STATUS_BAD)) continue;  // uniform over the CTA
+        const int32_t* list = b.bis_list + (int64_t)p * b.n_trial;
+        const float2* src = b.Wf2 + m.offf;  // padded to whole tiles
+        const int k = m.k_scan;
         const int q = c0 + e;
         const int j = q < ne ? list[q] : -1;
         if (tid == 0) s_jmax = -1;
@@ -614,6 +632,9 @@ __global__ void __launch_bounds__(kCountThreads) count_list_kernel(DevBatch b) {
     }
 }
 
+// (the count kernel's persistent grid: CTAs per SM)
+constexpr int kCountCtasPerSm = 8;
+
 template <int THREADS, int TILE, int STAGES>
 void launch_scan32_t(const DevBatch& b, int ctas_per_sm, int sm_count, cudaStream_t s, int stride) {
     const int ipp = ((b.n_trial + stride - 1) / stride + THREADS - 1) / THREADS;
@@ -659,13 +680,19 @@ void launch_scan64(const DevBatch& b, cudaStream_t s) {
 
 int scan32_max_tile() { return 4096; }
 
+// a round lists at most one entry per cell of width >= 2: n_trial / 2 per potential
+int64_t bisect_max_items(int n, int n_trial) {
+    return (int64_t)n * ((n_trial / 2 + kCountEnergies - 1) / kCountEnergies + 1);
+}
+
 void launch_bisect_scan(const DevBatch& b, const ScanShape& sh, int sm_count, cudaStream_t s) {
     cudaMemsetAsync(b.counts, 0xff, sizeof(int32_t) * (size_t)b.n * b.n_trial, s);  // -1: no count taken
     // the coarse grid with the throughput scan, then the bisection rounds
     launch_scan32(b, sh, sm_count, s, kBisectCoarse);
     for (int W = kBisectCoarse; W > 1; W /= 2) {
+        cudaMemsetAsync(&b.hdr->bis_items_n, 0, 2 * sizeof(int32_t), s);  // the round's items and queue
         bisect_plan_kernel<<<b.n, 256, 0, s>>>(b, W);
-        count_list_kernel<<<dim3(b.n, kCountSplit), kCountThreads, 0, s>>>(b);
+        count_list_kernel<<<sm_count * kCountCtasPerSm, kCountThreads, 0, s>>>(b);
     }
 }
 

@@ -228,6 +228,22 @@ epscu_status epscu_tabulate(epscu_ctx* ctx, int32_t n, const int32_t* kind, cons
                             const int64_t* offsets, const int32_t* N, const double* r_min,
                             const double* r_max, int32_t n_knots, double* V, const epscu_opts* opts);
 
+/* The adjoint of epscu_tabulate (same arguments and conventions): from
+ * dL_dV (the gradient of a loss with respect to the tabulated values V) it
+ * writes dL_dparams [n, 12] in the parameter layout of epscu_tabulate (zero
+ * where a kind has no parameter).  Morse and LJ rows take the analytic
+ * derivatives summed over the grid; Morse + bump rows go through the
+ * transpose of the natural-spline map from knots to grid (one tridiagonal
+ * sweep per potential) and then the knot values' derivatives.  One kernel,
+ * FP64, deterministic.  kind, offsets, N, r_min, r_max are host arrays;
+ * params, dL_dV and dL_dparams follow opts->flags (EPSCU_MEM_DEVICE).  No
+ * reference counterpart: the reference has no gradients (the forward is the
+ * MorsePotentialGenerator stub, potential_source.hpp:223-225). */
+epscu_status epscu_tabulate_adjoint(epscu_ctx* ctx, int32_t n, const int32_t* kind, const double* params,
+                                    const int64_t* offsets, const int32_t* N, const double* r_min,
+                                    const double* r_max, int32_t n_knots, const double* dL_dV, double* dL_dparams,
+                                    const epscu_opts* opts);
+
 /* Cooperative cancellation (TaskHandle::cancel,
  * cpp/gpu/include/epseon/gpu/task_handle.hpp:136-144).  Sets a host-mapped
  * flag that the persistent kernels poll between work items.  The request

@@ -201,3 +201,35 @@ def test_long_grid_top50_gradient(ctx):
     Em = O.solve_batch([V - hfd * d], b.r_min, b.r_max, b.mu, b.e_cap, b.n_trial, **kw)[0].energy_polished
     fd = float(np.sum(w * (Ep - Em)) / (2 * hfd))
     assert abs(an - fd) <= REL * abs(fd), (an, fd)
+
+
+def test_autograd_psi_exact_size_and_recompute():
+    """The autograd solve keeps its wavefunctions in a buffer of exactly the
+    size the levels need (sum over potentials of levels x grid points, read
+    back by the library after its level set-up), not capacity x points.  With
+    a memory budget below that size the forward keeps none and the backward
+    recomputes them in chunks of potentials that fit; the parameter gradients
+    agree with the stored-psi ones far below the finite-difference bar (the
+    chunks are re-solved as smaller batches, which may take a level through
+    the other pass of the same method: ~1e-12 relative)."""
+    b = synth.bump_adjoint(B=6, N=4096, n_trial=1024)
+    g = AG.Grids(b.N.copy(), b.r_min.copy(), b.r_max.copy(), b.mu.copy(), b.e_cap.copy(), b.n_trial, 128,
+                 capi.METHOD_FAST_FP32C)
+    P = torch.from_numpy(capi.batch_params(b)).cuda()
+    w = torch.from_numpy(synth.loss_weights(len(b) * 128).reshape(len(b), 128)).cuda()
+
+    def grads(solver):
+        Pr = P.clone().requires_grad_(True)
+        E, mask = AG.levels(AG.tabulate(Pr, b.kind, g, solver=solver), g, solver)
+        L = torch.sum(torch.where(mask, w * E, torch.zeros_like(E)))
+        rec = solver.last
+        L.backward()
+        return Pr.grad.cpu().numpy(), rec
+
+    stored, rec = grads(AG.Solver())
+    need = int(np.sum(rec.n_out.astype(np.int64) * b.N.astype(np.int64)))
+    assert rec.psi is not None and rec.psi.numel() == need == rec.psi_required
+    assert need < g.total * g.capacity // 2
+    recomputed, rec2 = grads(AG.Solver(psi_budget_bytes=need * 8 // 3))
+    assert rec2.psi is None and rec2.V is not None
+    assert np.max(np.abs(recomputed - stored)) <= 1e-10 * np.max(np.abs(stored))

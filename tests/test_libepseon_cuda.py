@@ -211,7 +211,7 @@ def test_nonuniform_file_matches_oracle(tmp_path):
     with open(f, "w") as fh:
         fh.write("# r[A]\tV[cm-1]\n")
         for x, y in zip(r, V):
-            fh.write(f"{x!r}\t{y!r}\n")
+            fh.write(f"{x:.17g}\t{y:.17g}\n")
     xs = r[0] + (r[-1] - r[0]) / (r.size - 1) * np.arange(r.size)
     xs[-1] = r[-1]
     Vu = scipy_interp.CubicSpline(r, V, bc_type="natural")(xs)
@@ -248,9 +248,10 @@ def test_group_size_splits_reproduce_unsplit_batch(precision):
     """HardwareConfig.group_size (hardware_config.hpp:16-18) is the number of
     potentials per device batch.  Splitting a batch into groups of 1 and 4
     reproduces the unsplit batch: bit for bit with the plain FP64 method (its
-    arithmetic is per potential), within 1e-10 Hartree with the fast method
-    (the long-window threshold follows the batch's level count, so a split
-    may route a level through the other pass of the same precision)."""
+    arithmetic is per potential, and the trial grid follows the whole task),
+    within 1e-10 Hartree with the fast method (the long-window threshold
+    follows the batch's level count, so a split may route a level through the
+    other pass of the same precision)."""
     m = _m()
     iface = _interface()
     out = {}
