@@ -252,7 +252,7 @@ def main():
                          "chosen from the level count)")
     ap.add_argument("--mid-window", type=int, default=0,
                     help="window length above which a level runs its double-float passes one warp per level "
-                         "(0: the library's default, < 0: no warp-per-level tier)")
+                         "(> 0; 0: the library's default, off)")
     ap.add_argument("--workload", default="mixed", choices=sorted(WORKLOADS),
                     help="mixed = the headline batch; the others are the single-Morse, 64-Morse, adjoint and "
                          "long-grid cases")

@@ -348,7 +348,7 @@ class Context:
         in place (for instance page-locked buffers reused across solves, so
         the device-to-host copies run at full speed); its psi is not used.
         wait_polls / max_iter: epscu_opts bounds (0: the defaults); mid_window:
-        the warp-per-level tier's threshold (0: default, < 0: off).
+        the warp-per-level tier's threshold (> 0; 0 or < 0: off, the default).
         check=False returns the Solution with the status code in .rc instead
         of raising on a non-zero code."""
         V, offsets, N = concat(Vs)

@@ -165,6 +165,9 @@ __device__ __forceinline__ int match_index(const PotMeta& m, const double* __res
 // bisection scan: the throughput scan on every kBisectCoarse-th trial
 // energy, then cells halved round by round
 constexpr int kBisectCoarse = 8;
+// points per cell and round of the bisection scan's rounds (a power of two
+// dividing kBisectCoarse)
+constexpr int kBisectSplit = 4;
 // batches of at least this many potentials take the bisection scan (smaller
 // ones have too few CTAs per round to cover its latency; measured on GB300)
 constexpr int kBisectMinPotentials = 512;

@@ -25,10 +25,13 @@ namespace epscu {
 constexpr int kLongWindow = 8192;
 constexpr int kLongWindowLevels = 60000;
 constexpr int kMinLongWindow = 1024;
-// windows above this many points (and up to the long-window threshold) run
-// their double-float passes one warp per level, after the lane FP32
-// refinement (DevBatch::mid_window overrides it; < 0 turns the tier off)
-constexpr int kMidWindow = 1024;
+// windows above this many points (and up to the long-window threshold) can
+// run their double-float passes one warp per level, after the lane FP32
+// refinement (DevBatch::mid_window > 0).  Off by default: on the
+// 2048-potential batch the warp passes (three marches of a chunked pass per
+// point) cost as much as the lane passes they replace (9 against 10 ms), and
+// the step was not shorter at thresholds of 1024 or 4096 points.
+constexpr int kMidWindow = -1;
 
 __host__ __device__ __forceinline__ int default_long_window(int total_levels) {
     int w = kMinLongWindow;

@@ -770,7 +770,9 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     // norm_long, twist_long, gather (+ zero_psi, scale_psi)
     const bool psi_kernels = psi_on;
     st.kernel_launches = method == EPSCU_METHOD_FAST_FP32C ? 17 + (psi_kernels ? 2 : 0) : 9 + (psi_kernels ? 1 : 0);
-    if (b.bis_list) st.kernel_launches += 6;  // three plan + count rounds after the coarse scan32
+    if (b.bis_list) {  // the plan + count rounds after the coarse scan32
+        for (int W = kBisectCoarse; W > 1; W /= (W < kBisectSplit ? W : kBisectSplit)) st.kernel_launches += 2;
+    }
     if (method == EPSCU_METHOD_PLAIN_FP64) {
         st.refine_point_updates = 0;
         int64_t bis = 0;

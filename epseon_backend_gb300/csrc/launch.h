@@ -54,6 +54,9 @@ struct DevBatch {
 };
 
 constexpr int kWaitPolls = 1 << 22;       // default bound of the TMA scan's mbarrier waits
+// persistent grid of the lane-per-level kernels: CTAs per SM launched (4 fit
+// at their register use; the rest start as the first ones finish)
+constexpr int kLaneCtasPerSm = 8;
 constexpr int kRefineMaxIter = 48;        // default cap on a level's FP32 refinement passes
 __device__ __forceinline__ int refine_cap(const DevBatch& b) { return b.max_iter > 0 ? b.max_iter : kRefineMaxIter; }
 // double-float fallback passes (bisection from the widened scan bracket)

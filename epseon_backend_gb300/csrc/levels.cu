@@ -557,7 +557,7 @@ void launch_bisect64(const DevBatch& b, int sm_count, cudaStream_t s) {
     bisect64_kernel<<<persistent_grid(sm_count, 8), kLevelThreads, 0, s>>>(b);
 }
 void launch_refine32(const DevBatch& b, int sm_count, cudaStream_t s) {
-    refine32_kernel<<<persistent_grid(sm_count, 8), kLevelThreads, 0, s>>>(b);
+    refine32_kernel<<<persistent_grid(sm_count, kLaneCtasPerSm), kLevelThreads, 0, s>>>(b);
 }
 void launch_norm64(const DevBatch& b, int use_k, int sm_count, cudaStream_t s) {
     norm64_kernel<<<persistent_grid(sm_count, 8), kLevelThreads, 0, s>>>(b, use_k);

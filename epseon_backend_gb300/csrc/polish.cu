@@ -466,10 +466,10 @@ void launch_scale_psi(const DevBatch& b, int sm_count, cudaStream_t s) {
 }
 
 void launch_newton_df(const DevBatch& b, int sm_count, cudaStream_t s) {
-    newton_df_kernel<<<sm_count * 8, kThreads, 0, s>>>(b);
+    newton_df_kernel<<<sm_count * kLaneCtasPerSm, kThreads, 0, s>>>(b);
 }
 void launch_norm_df(const DevBatch& b, int sm_count, cudaStream_t s) {
-    norm_df_kernel<<<sm_count * 8, kThreads, 0, s>>>(b);
+    norm_df_kernel<<<sm_count * kLaneCtasPerSm, kThreads, 0, s>>>(b);
 }
 void launch_write_df(const DevBatch& b, int sm_count, cudaStream_t s) {
     write_df_kernel<<<sm_count * 8, kThreads, 0, s>>>(b);

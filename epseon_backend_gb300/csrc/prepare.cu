@@ -456,7 +456,8 @@ __global__ void __launch_bounds__(128) window_kernel(DevBatch b, int sm_count) {
     const int total = b.hdr->total_levels;
     (void)sm_count;
     const int long_min = b.long_window > 0 ? b.long_window : default_long_window(total);
-    const int mid_min = b.mid_window < 0 || !b.mid_list ? 0x7fffffff : (b.mid_window > 0 ? b.mid_window : kMidWindow);
+    const int mid_w = b.mid_window != 0 ? b.mid_window : kMidWindow;
+    const int mid_min = mid_w <= 0 || !b.mid_list ? 0x7fffffff : mid_w;
     for (int slot = warp; slot < total; slot += n_warps) {
         const LevelWork w = b.levels[slot];
         if (w.status & EPSCU_STATUS_NOTFOUND) continue;

@@ -428,14 +428,15 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
 // potential instead of n_trial.  counts[] holds -1 where no count was taken.
 
 // The trial indices of the next round (W = 0: the coarse boundaries; else
-// the midpoints of the cells of width W whose end counts differ), and the
+// the split - 1 interior points that cut each cell of width W whose end counts
+// differ into `split` equal cells; split = 2 is bisection), and the
 // round's work items: the potential's list in chunks of kCountEnergies, so
 // that the count kernel runs every chunk of every potential side by side.
 // One CTA per potential, longest grids first (their items are listed first).
 constexpr int kCountThreads = 128;
 constexpr int kCountEnergies = kCountThreads / 2;
 
-__global__ void __launch_bounds__(256) bisect_plan_kernel(DevBatch b, int W) {
+__global__ void __launch_bounds__(256) bisect_plan_kernel(DevBatch b, int W, int split) {
     __shared__ int s_n;
     const int p = b.order[blockIdx.x];
     const PotMeta m = b.meta[p];
@@ -454,8 +455,11 @@ __global__ void __launch_bounds__(256) bisect_plan_kernel(DevBatch b, int W) {
                 const int a = t * W - 1;  // cell (a, a + W], count(-1) = 0
                 const int ca = a < 0 ? 0 : c[a];
                 const int cb = c[min(a + W, last)];
-                const int mid = a + W / 2;
-                if (ca >= 0 && cb > ca && mid < last) list[atomicAdd(&s_n, 1)] = mid;
+                if (ca >= 0 && cb > ca)
+                    for (int q = 1; q < split; ++q) {
+                        const int pt = a + q * (W / split);
+                        if (pt < last) list[atomicAdd(&s_n, 1)] = pt;
+                    }
             }
         }
     }
@@ -680,19 +684,27 @@ void launch_scan64(const DevBatch& b, cudaStream_t s) {
 
 int scan32_max_tile() { return 4096; }
 
-// a round lists at most one entry per cell of width >= 2: n_trial / 2 per potential
+// a round lists fewer than n_trial entries per potential
 int64_t bisect_max_items(int n, int n_trial) {
-    return (int64_t)n * ((n_trial / 2 + kCountEnergies - 1) / kCountEnergies + 1);
+    return (int64_t)n * ((n_trial + kCountEnergies - 1) / kCountEnergies + 1);
 }
 
 void launch_bisect_scan(const DevBatch& b, const ScanShape& sh, int sm_count, cudaStream_t s) {
     cudaMemsetAsync(b.counts, 0xff, sizeof(int32_t) * (size_t)b.n * b.n_trial, s);  // -1: no count taken
     // the coarse grid with the throughput scan, then the bisection rounds
     launch_scan32(b, sh, sm_count, s, kBisectCoarse);
-    for (int W = kBisectCoarse; W > 1; W /= 2) {
+    // each round cuts the cells that hold a level into kBisectSplit parts
+    // (the last round into what is left): with cells of 8 trial spacings,
+    // two rounds of 3 and 1 points per cell instead of three of 1.  Every
+    // round lasts about one march of its longest window, so fewer rounds with
+    // more counts each are shorter; the brackets are the same, and so is the
+    // bracket kernel's descent (every midpoint it visits has a count)
+    for (int W = kBisectCoarse; W > 1;) {
+        const int split = W < kBisectSplit ? W : kBisectSplit;
         cudaMemsetAsync(&b.hdr->bis_items_n, 0, 2 * sizeof(int32_t), s);  // the round's items and queue
-        bisect_plan_kernel<<<b.n, 256, 0, s>>>(b, W);
+        bisect_plan_kernel<<<b.n, 256, 0, s>>>(b, W, split);
         count_list_kernel<<<sm_count * kCountCtasPerSm, kCountThreads, 0, s>>>(b);
+        W /= split;
     }
 }
 

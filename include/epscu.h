@@ -119,10 +119,11 @@ typedef struct epscu_opts {
     int32_t max_iter;    /* fast method: cap on the FP32 refinement passes of a level and
                             on its double-float fallback passes (0: 48 and 96); a level
                             that reaches it carries EPSCU_LEVEL_MAXITER */
-    int32_t mid_window;  /* fast method: levels whose window exceeds this many points (and
-                            not the long-window threshold) run their double-float passes one
-                            warp per level after the lane FP32 refinement (0: 1024; < 0:
-                            never, they stay one lane per level) */
+    int32_t mid_window;  /* fast method: > 0: levels whose window exceeds this many points
+                            (and not the long-window threshold) run their double-float passes
+                            one warp per level after the lane FP32 refinement; 0 or < 0: off
+                            (the default: on the 2048-potential batch it did not shorten
+                            the solve) */
     epscu_alloc_fn psi_alloc;  /* EPSCU_MEM_DEVICE with EPSCU_WANT_PSI and result->psi NULL:
                                   the solve reads the wavefunctions' exact size back after
                                   its level set-up and asks psi_alloc for that buffer
