@@ -167,7 +167,7 @@ __device__ __forceinline__ int match_index(const PotMeta& m, const double* __res
 constexpr int kBisectCoarse = 8;
 // points per cell and round of the bisection scan's rounds (a power of two
 // dividing kBisectCoarse)
-constexpr int kBisectSplit = 4;
+constexpr int kBisectSplit = 8;
 // batches of at least this many potentials take the bisection scan (smaller
 // ones have too few CTAs per round to cover its latency; measured on GB300)
 constexpr int kBisectMinPotentials = 512;

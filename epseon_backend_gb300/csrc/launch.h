@@ -55,8 +55,9 @@ struct DevBatch {
 
 constexpr int kWaitPolls = 1 << 22;       // default bound of the TMA scan's mbarrier waits
 // persistent grid of the lane-per-level kernels: CTAs per SM launched (4 fit
-// at their register use; the rest start as the first ones finish)
-constexpr int kLaneCtasPerSm = 8;
+// at their register use; fewer leave room for the CTA-per-level branch that
+// runs beside them)
+constexpr int kLaneCtasPerSm = 4;
 constexpr int kRefineMaxIter = 48;        // default cap on a level's FP32 refinement passes
 __device__ __forceinline__ int refine_cap(const DevBatch& b) { return b.max_iter > 0 ? b.max_iter : kRefineMaxIter; }
 // double-float fallback passes (bisection from the widened scan bracket)
@@ -128,6 +129,7 @@ void launch_fallback_long(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_norm_long(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_write_long(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_twist_long(const DevBatch& b, int sm_count, cudaStream_t s);
+void longwin_set_attributes();  // the CTA kernels' dynamic shared memory (staged windows)
 void launch_refine_mid(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_norm_mid(const DevBatch& b, int sm_count, cudaStream_t s);
 
