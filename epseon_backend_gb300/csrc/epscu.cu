@@ -243,7 +243,6 @@ epscu_status epscu_create(int32_t device_ordinal, epscu_ctx** out) {
     }
     c->sm_count = p.multiProcessorCount;
     scan32_set_attributes();
-    longwin_set_attributes();
     *out = c;
     return EPSCU_OK;
 }

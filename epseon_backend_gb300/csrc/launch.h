@@ -129,7 +129,6 @@ void launch_fallback_long(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_norm_long(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_write_long(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_twist_long(const DevBatch& b, int sm_count, cudaStream_t s);
-void longwin_set_attributes();  // the CTA kernels' dynamic shared memory (staged windows)
 void launch_refine_mid(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_norm_mid(const DevBatch& b, int sm_count, cudaStream_t s);
 

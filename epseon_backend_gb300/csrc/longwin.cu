@@ -148,22 +148,6 @@ __device__ __forceinline__ void df_step(dfl T, dfl& A, dfl& D) {
     A = df_add(A, df_add(df_mul(T, A), D));
 }
 
-// ------------------------------------------------------------ the window
-// A level's a V pairs: in shared memory when its window was staged there
-// (element i at p[i - off]), else in global memory (off = 0).  Every pass of a
-// level marches the same window [j0, j1], so a CTA-per-level kernel copies it
-// into shared memory once per level and the passes' dependent steps never
-// wait on an L2 or HBM load.
-struct WinW {
-    const float2* p;
-    int off;
-    __device__ __forceinline__ float2 operator()(int i) const { return p[i - off]; }
-};
-
-// points of a window that fit the dynamic shared memory of a CTA kernel
-// (96 KiB: two CTAs of kLongThreads per SM); longer windows read global memory
-constexpr int kWinPoints = 12288;
-
 // ---------------------------------------------------------------- groups
 // A level's passes run on a group of NW warps (NW = 8: the whole CTA of
 // kLongThreads; NW = 1: one warp, kLongThreads / 32 groups per CTA).  The
@@ -317,7 +301,7 @@ struct TwistIO {
 };
 
 template <int NW, int MODE>
-__device__ LongSide<MODE> long_side(const Grp<NW>& G, WinW Wf, dfl aE, int from, int to,
+__device__ LongSide<MODE> long_side(const Grp<NW>& G, const float2* __restrict__ Wf, dfl aE, int from, int to,
                                     int dir, double* __restrict__ out, double L, int Xk, SharedDF<NW>& sh,
                                     TwistIO* tw = nullptr) {
     // MODE 0: state, 1: + sums/peak, 2: + psi write, 3: MODE 1 + unnormalised
@@ -353,7 +337,7 @@ __device__ LongSide<MODE> long_side(const Grp<NW>& G, WinW Wf, dfl aE, int from,
         dfl A1 = {1.0f, 0.0f}, D1 = {0.0f, 0.0f}, A2 = {0.0f, 0.0f}, D2 = {1.0f, 0.0f};
         int e = 0;
         for (int st = s0; st < s1; ++st) {
-            const dfl T = t_of(aE, Wf(from + dir * st));
+            const dfl T = t_of(aE, __ldg(Wf + from + dir * st));
             if (kPsi) P.v = df_mul(P.v, df_recip(df_add({1.0f, 0.0f}, T)));
             df_step(T, A1, D1);
             df_step(T, A2, D2);
@@ -443,7 +427,7 @@ __device__ LongSide<MODE> long_side(const Grp<NW>& G, WinW Wf, dfl aE, int from,
     int g_k = 0x7fffffff;
     for (int st = s0; st < s1; ++st) {
         const int i = from + dir * st;
-        const dfl T = t_of(aE, Wf(i));
+        const dfl T = t_of(aE, __ldg(Wf + i));
         if (MODE == 4 || MODE == 5) {
             // twist search samples, before the step at i: outward, D/A of the
             // outward state; inward, gamma_i = -12 T_i / f_i + (D/A)_out +
@@ -612,7 +596,7 @@ __device__ LongSide<MODE> long_side(const Grp<NW>& G, WinW Wf, dfl aE, int from,
 // unnormalised psi-hat of the window in row (if not null).
 template <int NW, int MODE>
 __device__ __forceinline__ PassDF long_pass(const Grp<NW>& G, const PotMeta& m, const LevelWork& w,
-                                            WinW Wf, const double* __restrict__ W64, double E,
+                                            const float2* __restrict__ Wf, const double* __restrict__ W64, double E,
                                             int k, double sum_fallback, SharedDF<NW>& sh,
                                             double* __restrict__ row = nullptr) {
     if (G.leader()) sh.aE = energy_df(m, E);
@@ -754,7 +738,7 @@ struct LongSide32 {
 // carried to the side's end by the product of F over the later chunks.  The
 // result is valid in the leader.
 template <int NW>
-__device__ LongSide32 long_side32(const Grp<NW>& G, WinW Wf, float aEh, float aEl, int from,
+__device__ LongSide32 long_side32(const Grp<NW>& G, const float2* __restrict__ Wf, float aEh, float aEl, int from,
                                   int to, int dir, Shared32<NW>& sh) {
     constexpr int kT = Grp<NW>::kThreads;
     const int tid = G.t(), lane = G.lane(), warp = G.warp();
@@ -780,7 +764,7 @@ __device__ LongSide32 long_side32(const Grp<NW>& G, WinW Wf, float aEh, float aE
         float A1 = 1.0f, D1 = 0.0f, A2 = 0.0f, D2 = 1.0f;
         int e = 0;
         for (int st = s0; st < s1; ++st) {
-            const float2 w = Wf(from + dir * st);
+            const float2 w = __ldg(Wf + from + dir * st);
             const float T = (aEh - w.x) + (aEl - w.y);
             const float f = 1.0f + T;
             F.v *= f * f;
@@ -866,7 +850,7 @@ __device__ LongSide32 long_side32(const Grp<NW>& G, WinW Wf, float aEh, float aE
     int nodes = 0;
     int peak_L = -(1 << 30), peak_s = 0x7fffffff;
     for (int st = s0; st < s1; ++st) {
-        const float2 w = Wf(from + dir * st);
+        const float2 w = __ldg(Wf + from + dir * st);
         const float T = (aEh - w.x) + (aEl - w.y);
         const float f = 1.0f + T;
         S = fmaf(f * f, S, A * A);
@@ -954,7 +938,7 @@ __device__ LongSide32 long_side32(const Grp<NW>& G, WinW Wf, float aEh, float aE
 // formed by the leader and handed to the group.
 template <int NW>
 __device__ __forceinline__ PassDF long_pass32(const Grp<NW>& G, const PotMeta& m, const LevelWork& w,
-                                              WinW Wf, const double* __restrict__ W64,
+                                              const float2* __restrict__ Wf, const double* __restrict__ W64,
                                               double E, int k, Shared32<NW>& sh) {
     if (G.leader()) {
         const double aE = __dmul_rn(m.a, E);
@@ -990,21 +974,6 @@ __device__ __forceinline__ PassDF long_pass32(const Grp<NW>& G, const PotMeta& m
     }
     gsync<NW>();
     return sh.res;
-}
-
-// Stages the level's window of a V pairs [j0, j1] in shared memory when it fits
-// (CTA groups only): vector loads of two points from an even start, so the
-// copy stays 16-byte aligned and inside the potential's tile-padded pairs.
-template <int NW>
-__device__ __forceinline__ WinW stage_window(const Grp<NW>& G, const float2* Wg, const LevelWork& w, float2* wsh) {
-    const int a0 = w.j0 & ~1;
-    const int cnt = w.j1 + 1 - a0;
-    if (NW != kLongWarps || wsh == nullptr || cnt > kWinPoints) return {Wg, 0};
-    const float4* src = reinterpret_cast<const float4*>(Wg + a0);
-    float4* dst = reinterpret_cast<float4*>(wsh);
-    for (int q = G.t(); q < (cnt + 1) / 2; q += Grp<NW>::kThreads) dst[q] = __ldg(src + q);
-    gsync<NW>();
-    return {wsh, a0};
 }
 
 // the host-mapped cancel flag, read by the leader and handed to the group
@@ -1043,11 +1012,9 @@ __global__ void __launch_bounds__(kLongThreads) refine_long_kernel(DevBatch b, i
     constexpr int kG = kLongThreads / (32 * NW);
     __shared__ SharedDF<NW> shd[kG];
     __shared__ Shared32<NW> sh32s[kG];
-    extern __shared__ __align__(16) unsigned char lw_dyn[];  // the staged window (CTA groups)
     const Grp<NW> G;
     SharedDF<NW>& sh = shd[G.g()];
     Shared32<NW>& sh32 = sh32s[G.g()];
-    float2* wsh = NW == kLongWarps ? reinterpret_cast<float2*>(lw_dyn) : nullptr;
     const int n = min(*list_len, b.max_levels);  // filled on the device earlier in the solve
     // levels from a device queue (a group takes the next as it finishes one)
     for (;;) {
@@ -1061,7 +1028,7 @@ __global__ void __launch_bounds__(kLongThreads) refine_long_kernel(DevBatch b, i
             continue;
         }
         const PotMeta m = b.meta[w.p];
-        const WinW Wf = stage_window<NW>(G, b.Wf2 + m.offf, w, wsh);
+        const float2* Wf = b.Wf2 + m.offf;
         const double* W = b.W64 + m.off;
         double lo = w.lo, hi = w.hi, E = w.E, sum = 1.0;
         int k = mode == 2 ? w.k : grp_bcast<NW>(G, G.leader() ? clamp_k(w, match_index(m, b.Msuf, E)) : 0, sh.word);
@@ -1210,10 +1177,8 @@ __global__ void __launch_bounds__(kLongThreads) norm_long_kernel(DevBatch b, con
                                                                  const int32_t* list_len, int qid) {
     constexpr int kG = kLongThreads / (32 * NW);
     __shared__ SharedDF<NW> shd[kG];
-    extern __shared__ __align__(16) unsigned char lw_dyn[];  // the staged window (CTA groups)
     const Grp<NW> G;
     SharedDF<NW>& sh = shd[G.g()];
-    float2* wsh = NW == kLongWarps ? reinterpret_cast<float2*>(lw_dyn) : nullptr;
     const int n = min(*list_len, b.max_levels);
     for (;;) {
         const int q = grp_next<NW>(G, &b.hdr->queue[qid], sh.word);
@@ -1222,7 +1187,7 @@ __global__ void __launch_bounds__(kLongThreads) norm_long_kernel(DevBatch b, con
         LevelWork w = b.levels[slot];
         if (w.status & (EPSCU_STATUS_NOTFOUND | EPSCU_STATUS_CANCELLED)) continue;
         const PotMeta m = b.meta[w.p];
-        const WinW Wf = stage_window<NW>(G, b.Wf2 + m.offf, w, wsh);
+        const float2* Wf = b.Wf2 + m.offf;
         const double* W = b.W64 + m.off;
         double* row = psi_row(b, m, w);
         auto pass = [&](int kk) { return long_pass<NW, 3>(G, m, w, Wf, W, w.E, kk, 1.0, sh, row); };
@@ -1283,7 +1248,7 @@ __global__ void __launch_bounds__(kLongThreads) twist_long_kernel(DevBatch b) {
         const int slot = b.twist_list[q];
         LevelWork w = b.levels[slot];
         const PotMeta m = b.meta[w.p];
-        const WinW Wf{b.Wf2 + m.offf, 0};
+        const float2* Wf = b.Wf2 + m.offf;
         const double* W = b.W64 + m.off;
         const dfl aE = energy_df(m, w.E);
         TwistIO tw;
@@ -1339,7 +1304,7 @@ __global__ void __launch_bounds__(kLongThreads) write_long_kernel(DevBatch b, co
         double* out = b.psi + m.psi_off + (int64_t)(w.v - b.min_level) * m.N;
         // the rows were zeroed by zero_psi: only the window is written
         if (no_result(w)) continue;
-        const WinW Wf{b.Wf2 + m.offf, 0};
+        const float2* Wf = b.Wf2 + m.offf;
         const dfl aE = energy_df(m, w.E);
         long_side<kLongWarps, 2>(G, Wf, aE, w.j0, w.k, +1, out, w.norm_k_out, w.ex_out, sh);
         long_side<kLongWarps, 2>(G, Wf, aE, w.j1, w.k, -1, out, w.norm_k_in, w.ex_in, sh);
@@ -1350,27 +1315,19 @@ __global__ void __launch_bounds__(kLongThreads) write_long_kernel(DevBatch b, co
 
 }  // namespace
 
-constexpr size_t kWinBytes = sizeof(float2) * kWinPoints;
-
-void longwin_set_attributes() {
-    cudaFuncSetAttribute(refine_long_kernel<kLongWarps>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWinBytes);
-    cudaFuncSetAttribute(norm_long_kernel<kLongWarps>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWinBytes);
-}
-
 void launch_refine_long(const DevBatch& b, int sm_count, cudaStream_t s) {
     if (!b.long_list) return;
     refine_long_kernel<kLongWarps>
-        <<<sm_count * 2, kLongThreads, kWinBytes, s>>>(b, 0, b.long_list, &b.hdr->n_long, kQLongRefine);
+        <<<sm_count * 2, kLongThreads, 0, s>>>(b, 0, b.long_list, &b.hdr->n_long, kQLongRefine);
 }
 void launch_fallback_long(const DevBatch& b, int sm_count, cudaStream_t s) {
     if (!b.fallback_list) return;
     refine_long_kernel<kLongWarps>
-        <<<sm_count * 2, kLongThreads, kWinBytes, s>>>(b, 1, b.fallback_list, &b.hdr->fallbacks, kQFallback);
+        <<<sm_count * 2, kLongThreads, 0, s>>>(b, 1, b.fallback_list, &b.hdr->fallbacks, kQFallback);
 }
 void launch_norm_long(const DevBatch& b, int sm_count, cudaStream_t s) {
     if (!b.long_list) return;
-    norm_long_kernel<kLongWarps>
-        <<<sm_count * 2, kLongThreads, kWinBytes, s>>>(b, b.long_list, &b.hdr->n_long, kQNormLong);
+    norm_long_kernel<kLongWarps><<<sm_count * 2, kLongThreads, 0, s>>>(b, b.long_list, &b.hdr->n_long, kQNormLong);
 }
 void launch_twist_long(const DevBatch& b, int sm_count, cudaStream_t s) {
     if (!b.twist_list || !b.long_list) return;
