@@ -94,7 +94,7 @@ struct Header {
 
 // queue ids of the per-level kernels
 enum { kQRefine32 = 0, kQNewtonDF, kQNormDF, kQWriteDF, kQBisect64, kQNorm64, kQWrite64, kQLongRefine, kQFallback,
-       kQNormLong, kQTwistLong, kQMidRefine, kQNormMid };
+       kQNormLong, kQTwistLong, kQMidRefine, kQNormMid, kQScalePsi };
 
 // internal level flags (not reported: gather keeps the public bits only)
 // the Newton stage handed the level to the fallback

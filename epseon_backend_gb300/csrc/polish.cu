@@ -409,20 +409,26 @@ __global__ void __launch_bounds__(256) zero_psi_kernel(DevBatch b) {
 // window point).
 __global__ void __launch_bounds__(256) scale_psi_kernel(DevBatch b) {
     if (!b.psi || b.hdr->error) return;
-    const int lane = threadIdx.x & 31;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int n_warps = (gridDim.x * blockDim.x) >> 5;
+    __shared__ int s_slot;
     const int total = b.hdr->total_levels;
     unsigned long long converted = 0;
-    for (int slot = warp; slot < total; slot += n_warps) {
+    // levels from a device queue, one CTA each: the windows range from a few
+    // hundred to ~6.5e4 points, and a warp per level handed out round-robin
+    // left the SMs busy only ~40% of the kernel (ncu)
+    for (;;) {
+        if (threadIdx.x == 0) s_slot = atomicAdd(&b.hdr->queue[kQScalePsi], 1);
+        __syncthreads();
+        const int slot = s_slot;
+        __syncthreads();  // every thread has read s_slot
+        if (slot >= total) break;
         const LevelWork w = b.levels[slot];
         const PotMeta m = b.meta[w.p];
         double* row = b.psi + m.psi_off + (int64_t)(w.v - b.min_level) * m.N;
         if (no_result(w)) {
-            for (int i = w.j0 + lane; i <= w.j1; i += 32) row[i] = 0.0;
+            for (int i = w.j0 + (int)threadIdx.x; i <= w.j1; i += blockDim.x) row[i] = 0.0;
             continue;
         }
-        converted += (unsigned long long)(w.j1 - w.j0 + 1);
+        if (threadIdx.x == 0) converted += (unsigned long long)(w.j1 - w.j0 + 1);
         // the side constants norm_k 2^-ex as m 2^e, m in [0.5, 1) a
         // double-float: per point the pair times m in double-float and the
         // double assembled with integer operations, scaled by 2^(64 r + e)
@@ -440,19 +446,20 @@ __global__ void __launch_bounds__(256) scale_psi_kernel(DevBatch b) {
             const dfl p = df_mul(v, outward ? M_out : M_in);
             return i == w.k ? w.ck : df_pair_to_double_scaled(p.h, p.l, 64 * r + (outward ? e_out : e_in));
         };
-        // four points per lane per step: four loads in flight (the kernel is
-        // bound by HBM latency with one)
-        int i = w.j0 + lane;
-        for (; i + 96 <= w.j1; i += 128) {
-            const float2 r0 = pair[i], r1 = pair[i + 32], r2 = pair[i + 64], r3 = pair[i + 96];
+        // four points per thread per step (four loads in flight), the CTA's
+        // 256 threads coalesced over the window
+        constexpr int kS = 256;
+        int i = w.j0 + (int)threadIdx.x;
+        for (; i + 3 * kS <= w.j1; i += 4 * kS) {
+            const float2 r0 = pair[i], r1 = pair[i + kS], r2 = pair[i + 2 * kS], r3 = pair[i + 3 * kS];
             row[i] = convert(i, r0);
-            row[i + 32] = convert(i + 32, r1);
-            row[i + 64] = convert(i + 64, r2);
-            row[i + 96] = convert(i + 96, r3);
+            row[i + kS] = convert(i + kS, r1);
+            row[i + 2 * kS] = convert(i + 2 * kS, r2);
+            row[i + 3 * kS] = convert(i + 3 * kS, r3);
         }
-        for (; i <= w.j1; i += 32) row[i] = convert(i, pair[i]);
+        for (; i <= w.j1; i += kS) row[i] = convert(i, pair[i]);
     }
-    if (lane == 0 && converted) atomicAdd(&b.hdr->psi_window_points, converted);
+    if (threadIdx.x == 0 && converted) atomicAdd(&b.hdr->psi_window_points, converted);
 }
 
 }  // namespace

@@ -685,7 +685,8 @@ __global__ void __launch_bounds__(kTabAdjThreads) tabulate_adjoint_kernel(
         __syncthreads();
         // ---- dL/dy_k = (P^T g)_k + s6 (D2^T z)_k, then the knots' parameter derivatives
         for (int kk = threadIdx.x; kk < K; kk += kTabAdjThreads) {
-            double gy = Ly[kk] + (kk > 0 ? Ry[kk - 1] : 0.0);
+            // (intervals are 0..K-2: the last knot has no interval of its own)
+            double gy = (kk < K - 1 ? Ly[kk] : 0.0) + (kk > 0 ? Ry[kk - 1] : 0.0);
             const double zl = kk >= 1 ? z[kk - 1] : 0.0, zc = z[kk], zr = kk + 1 < K ? z[kk + 1] : 0.0;
             gy += s6 * (zl - 2.0 * zc + zr);
             const double r = r0 + kk * hk;
