@@ -5,14 +5,18 @@
 // exactly dE_v / dV_i = psi_v(r_i)^2 h for the wavefunction normalised with
 // sum psi^2 h = 1, so for L(E) the gradient is
 //     dL/dV_i = sum_v dL/dE_v psi_v(r_i)^2 h.
-// One thread per grid point, reading the potential's psi rows coalesced; the
-// kernel is HBM-bound (8 bytes of psi per level and point).  psi is zero
+// One thread per grid point, reading the potential's psi rows coalesced.  The
+// sum runs in double-float on the FP32 pipes (each psi double split into a
+// float pair by its bits, dL/dE_v psi^2 by two-product arithmetic, ~1e-14
+// relative): with an FP64 multiply-add per level and point the kernel was
+// bound by GB300's FP64 pipe (ncu: 82% busy), not by HBM.  psi is zero
 // outside each level's window [j0, j1] (the written rows hold zeros there), so
 // those reads are skipped: on the mixed batch the fast method's windows hold
 // about a fifth of the row points.
 #include <cuda_runtime.h>
 
 #include "common.cuh"
+#include "dfloat.cuh"
 #include "launch.h"
 
 namespace epscu {
@@ -33,7 +37,7 @@ __global__ void __launch_bounds__(256) adjoint_kernel(DevBatch b, const double* 
                                                       int accumulate) {
     __shared__ int s_lo, s_hi;
     __shared__ int2 s_win[kAdjTile];
-    __shared__ double s_g[kAdjTile];
+    __shared__ float s_gh[kAdjTile], s_gl[kAdjTile];  // dL/dE as double-float pairs
     const int p = blockIdx.y;
     const PotMeta m = b.meta[p];
     const int i_a = blockIdx.x * blockDim.x;
@@ -56,13 +60,15 @@ __global__ void __launch_bounds__(256) adjoint_kernel(DevBatch b, const double* 
     const int i = i_a + threadIdx.x;
     const double* rows = psi + m.psi_off + i;
     const double* g = gE + (int64_t)p * b.level_capacity;
-    double acc = 0.0;
+    dfl acc = {0.0f, 0.0f};
     for (int t0 = lo; t0 <= hi; t0 += kAdjTile) {
         const int nt = min(kAdjTile, hi - t0 + 1);
         __syncthreads();  // the previous round's stage is consumed
         for (int q = threadIdx.x; q < nt; q += blockDim.x) {
             s_win[q] = make_int2(lw[t0 + q].j0, lw[t0 + q].j1);
-            s_g[q] = g[t0 + q];
+            const dfl gq = df_from_double(g[t0 + q]);
+            s_gh[q] = gq.h;
+            s_gl[q] = gq.l;
         }
         __syncthreads();
         if (i > i_b) continue;
@@ -73,7 +79,11 @@ __global__ void __launch_bounds__(256) adjoint_kernel(DevBatch b, const double* 
             return i >= wq.x && i <= wq.y;
         };
         auto load = [&](int q) { return inside(q) ? __ldg(rows + (int64_t)(t0 + q) * m.N) : 0.0; };
-        auto add = [&](int q, double v) { acc = inside(q) ? fma(s_g[q] * v, v, acc) : acc; };
+        auto add = [&](int q, double v) {
+            if (!inside(q)) return;
+            const dfl x = df_split_double_bits(v);
+            acc = df_add(acc, df_mul(df_mul(x, x), dfl{s_gh[q], s_gl[q]}));
+        };
         int q = 0;
         for (; q + 3 < nt; q += 4) {
             const double v0 = load(q), v1 = load(q + 1), v2 = load(q + 2), v3 = load(q + 3);
@@ -85,9 +95,9 @@ __global__ void __launch_bounds__(256) adjoint_kernel(DevBatch b, const double* 
         for (; q < nt; ++q) add(q, load(q));
     }
     if (i > i_b) return;
-    acc *= m.h;
-    if (accumulate) gV[offsets[p] + i] += acc;
-    else gV[offsets[p] + i] = acc;
+    const double r = (f2d(acc.h) + f2d(acc.l)) * m.h;
+    if (accumulate) gV[offsets[p] + i] += r;
+    else gV[offsets[p] + i] = r;
 }
 
 // Explicit layout (stateless adjoint): per-potential arrays on the device.

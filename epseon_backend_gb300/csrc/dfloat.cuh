@@ -177,6 +177,25 @@ __device__ __forceinline__ double df_pair_to_double_scaled(float h, float l, int
     return ldexp(d, e2);
 }
 
+// A double as a double-float pair (h + l, ~48 significant bits) through its
+// bit pattern on the integer pipe: h keeps the top 24 significand bits, l the
+// next 29 (converted once).  No FP64 instruction.  Zero, subnormal and very
+// small or large |x| (outside 2^+-100) give a zero pair: the callers square
+// and weight values whose useful range is far inside that.
+__device__ __forceinline__ dfl df_split_double_bits(double x) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    const uint32_t hi = (uint32_t)(u >> 32), lo = (uint32_t)u;
+    const int e = (int)((hi >> 20) & 0x7ffu) - 1023;
+    if (e < -100 || e > 100) return {0.0f, 0.0f};
+    const uint32_t sgn = hi & 0x80000000u;
+    const uint32_t top23 = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const float h = __uint_as_float(sgn | ((uint32_t)(e + 127) << 23) | top23);
+    // the remaining 29 bits are worth (lo & (2^29 - 1)) 2^(e - 52)
+    float l = __uint2float_rn(lo & 0x1fffffffu) * 2.220446049250313e-16f;  // 2^-52 (a normal float)
+    l = __fmul_rn(l, __int_as_float((127 + e) << 23));                    // 2^e, |e| <= 100
+    return {h, sgn ? -l : l};
+}
+
 __device__ __forceinline__ dfl df_from_double(double x) {
     const float h = __double2float_rn(x);
     const float l = __double2float_rn(x - (double)h);
