@@ -47,6 +47,18 @@ struct OrI {
     __device__ int operator()(int a, int b) const { return a | b; }
 };
 
+// An unsigned integer image of a double that orders like the double (for
+// non-NaN values): minima taken on it are exact and need no FP64 instruction.
+constexpr unsigned long long kKeyMax = ~0ull;  // above every image (+inf's image is below it)
+__device__ __forceinline__ unsigned long long dkey(double x) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double dkey_inv(unsigned long long k) {
+    const unsigned long long u = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+    return __longlong_as_double((long long)u);
+}
+
 __global__ void __launch_bounds__(kPrepThreads) prepare_kernel(DevBatch b) {
     __shared__ double shd[32];
     __shared__ int shi[32];
@@ -107,58 +119,61 @@ __global__ void __launch_bounds__(kPrepThreads) prepare_kernel(DevBatch b) {
         }
     }
 
-    // suffix minima of V on [i0, i1] (chunked block scan, right to left)
-    __shared__ double chunk_min[kPrepThreads];
-    const int n_in = i1 - i0 + 1;
-    const int per = n_in > 0 ? (n_in + nt - 1) / nt : 0;
-    const int c0 = i0 + tid * per;
-    const int c1 = min(c0 + per, i1 + 1);
-    double cm = INFINITY;
-    for (int i = c0; i < c1; ++i) cm = fmin(cm, V[i]);
-    chunk_min[tid] = cm;
-    __syncthreads();
-    if (tid == 0) {
-        double run = INFINITY;
-        for (int t = nt - 1; t >= 0; --t) {
-            const double x = chunk_min[t];
-            chunk_min[t] = run;  // minimum of all chunks to the right of t
-            run = fmin(run, x);
-        }
-    }
-    __syncthreads();
-    double* M = b.Msuf + m.off;
-    double run = chunk_min[tid];
-    for (int i = c1 - 1; i >= c0; --i) {
-        run = fmin(run, V[i]);
-        M[i] = run;
-    }
-
-    if (b.Mpre) {
-        // prefix minima (left to right) and minima of a V over 32-point blocks
-        // clipped to [i0, i1], rounded down to float: the decay-window bounds
+    // Suffix minima of V on [i0, i1] (M), and for the fast method prefix
+    // minima (P) and the minima of a V over 32-point blocks clipped to
+    // [i0, i1], rounded down to float (the decay-window bounds).  Coalesced
+    // warp scans over the absolute 32-point blocks B0..B1: each warp owns a
+    // contiguous run of blocks and scans it with shuffles, seeded with the
+    // minimum of the runs to its right (suffix) or left (prefix).  Minima are
+    // taken on an order-preserving integer image of the doubles (exact, and
+    // no FP64 instruction at GB300's 1/64 rate).
+    {
+        const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+        const int B0 = i0 >> 5, B1 = i1 >> 5, nblk = i1 >= i0 ? B1 - B0 + 1 : 0;
+        const int per = (nblk + nw - 1) / nw;
+        const int wb0 = B0 + min(warp * per, nblk), wb1 = B0 + min((warp + 1) * per, nblk);  // [wb0, wb1)
+        __shared__ unsigned long long s_run[32];
+        auto load_key = [&](int B) {
+            const int idx = (B << 5) + lane;
+            return (idx >= i0 && idx <= i1) ? dkey(V[idx]) : kKeyMax;
+        };
+        // this warp's run minimum
+        unsigned long long rm = kKeyMax;
+        for (int B = wb0; B < wb1; ++B) rm = min(rm, load_key(B));
+        for (int o = 16; o > 0; o >>= 1) rm = min(rm, __shfl_xor_sync(0xffffffffu, rm, o));
+        if (lane == 0) s_run[warp] = rm;
         __syncthreads();
-        chunk_min[tid] = cm;
-        __syncthreads();
-        if (tid == 0) {
-            double acc = INFINITY;
-            for (int t = 0; t < nt; ++t) {
-                const double x = chunk_min[t];
-                chunk_min[t] = acc;  // minimum of all chunks to the left of t
-                acc = fmin(acc, x);
+        double* M = b.Msuf + m.off;
+        unsigned long long carry = kKeyMax;  // the minimum right of this warp's run
+        for (int w = warp + 1; w < nw; ++w) carry = min(carry, s_run[w]);
+        float* Bm = b.Mpre ? b.Bmin + m.offf / 32 : nullptr;
+        for (int B = wb1 - 1; B >= wb0; --B) {
+            unsigned long long k = load_key(B);
+            // inclusive suffix minimum over the lanes (lane l: lanes l..31)
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned long long y = __shfl_down_sync(0xffffffffu, k, o);
+                if (lane + o < 32) k = min(k, y);
             }
+            const unsigned long long blk = __shfl_sync(0xffffffffu, k, 0);  // the block's minimum
+            const int idx = (B << 5) + lane;
+            if (idx >= i0 && idx <= i1) M[idx] = dkey_inv(min(k, carry));
+            if (Bm && lane == 0) Bm[B] = __double2float_rd(__dmul_rn(a, dkey_inv(blk)));
+            carry = min(carry, blk);
         }
-        __syncthreads();
-        double* P = b.Mpre + m.off;
-        double pr = chunk_min[tid];
-        for (int i = c0; i < c1; ++i) {
-            pr = fmin(pr, V[i]);
-            P[i] = pr;
-        }
-        float* Bm = b.Bmin + m.offf / 32;
-        for (int B = (i0 >> 5) + tid; B <= (i1 >> 5); B += nt) {
-            double vb = INFINITY;
-            for (int i = max(B << 5, i0); i <= min((B << 5) + 31, i1); ++i) vb = fmin(vb, V[i]);
-            Bm[B] = __double2float_rd(__dmul_rn(a, vb));
+        if (b.Mpre) {
+            double* P = b.Mpre + m.off;
+            carry = kKeyMax;  // the minimum left of this warp's run
+            for (int w = 0; w < warp; ++w) carry = min(carry, s_run[w]);
+            for (int B = wb0; B < wb1; ++B) {
+                unsigned long long k = load_key(B);
+                for (int o = 1; o < 32; o <<= 1) {
+                    const unsigned long long y = __shfl_up_sync(0xffffffffu, k, o);
+                    if (lane >= o) k = min(k, y);
+                }
+                const int idx = (B << 5) + lane;
+                if (idx >= i0 && idx <= i1) P[idx] = dkey_inv(min(k, carry));
+                carry = min(carry, __shfl_sync(0xffffffffu, k, 31));
+            }
         }
     }
 
