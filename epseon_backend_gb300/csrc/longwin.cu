@@ -1338,12 +1338,17 @@ void launch_write_long(const DevBatch& b, int sm_count, cudaStream_t s) {
     if (b.long_list) write_long_kernel<<<sm_count * 2, kLongThreads, 0, s>>>(b, b.long_list, &b.hdr->n_long);
     if (b.mid_list) write_long_kernel<<<sm_count * 2, kLongThreads, 0, s>>>(b, b.mid_list, &b.hdr->n_mid);
 }
+// the middle tier is in use (its list can be non-empty): the same threshold
+// as the window kernel's
+static bool mid_tier_on(const DevBatch& b) {
+    return b.mid_list && (b.mid_window != 0 ? b.mid_window : kMidWindow) > 0;
+}
 void launch_refine_mid(const DevBatch& b, int sm_count, cudaStream_t s) {
-    if (!b.mid_list) return;
+    if (!mid_tier_on(b)) return;
     refine_long_kernel<1><<<sm_count * 2, kLongThreads, 0, s>>>(b, 2, b.mid_list, &b.hdr->n_mid, kQMidRefine);
 }
 void launch_norm_mid(const DevBatch& b, int sm_count, cudaStream_t s) {
-    if (!b.mid_list) return;
+    if (!mid_tier_on(b)) return;
     norm_long_kernel<1><<<sm_count * 2, kLongThreads, 0, s>>>(b, b.mid_list, &b.hdr->n_mid, kQNormMid);
 }
 
