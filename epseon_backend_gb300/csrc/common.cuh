@@ -168,6 +168,11 @@ constexpr int kBisectCoarse = 8;
 // points per cell and round of the bisection scan's rounds (a power of two
 // dividing kBisectCoarse)
 constexpr int kBisectSplit = 8;
+// parts a coarse cell that holds exactly one level is cut into (a power of
+// two dividing kBisectCoarse; 1: no count inside, the level's bracket is the
+// whole cell, which isolates it already).  Cells with two or more levels are
+// cut into kBisectSplit parts round by round.
+constexpr int kBisectSingle = 2;
 // batches of at least this many potentials take the bisection scan (smaller
 // ones have too few CTAs per round to cover its latency; measured on GB300)
 constexpr int kBisectMinPotentials = 512;

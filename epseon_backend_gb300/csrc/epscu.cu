@@ -765,11 +765,13 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     st.psi_bytes = psi_on ? psi_total * 8 : 0;
     // plain: prepare, scan64, level/unit setup, bracket, bisect64, norm64,
     // twist64, gather (+ write64); fast: prepare, scan window, scan32, level/unit
-    // setup, bracket, window, refine32, refine_long, refine_mid, newton_df,
-    // fallback (refine_long over the fallback list), norm_mid, norm_df,
-    // norm_long, twist_long, gather (+ zero_psi, scale_psi)
+    // setup, bracket, window, refine32, refine_long, newton_df, fallback
+    // (refine_long over the fallback list), norm_df, norm_long, twist_long,
+    // gather (+ refine_mid, norm_mid with the middle tier; + zero_psi, scale_psi)
     const bool psi_kernels = psi_on;
-    st.kernel_launches = method == EPSCU_METHOD_FAST_FP32C ? 17 + (psi_kernels ? 2 : 0) : 9 + (psi_kernels ? 1 : 0);
+    const bool mid_on = b.mid_list && (b.mid_window != 0 ? b.mid_window : kMidWindow) > 0;
+    st.kernel_launches = method == EPSCU_METHOD_FAST_FP32C ? 15 + (mid_on ? 2 : 0) + (psi_kernels ? 2 : 0)
+                                                           : 9 + (psi_kernels ? 1 : 0);
     if (b.bis_list) {  // the plan + count rounds after the coarse scan32
         for (int W = kBisectCoarse; W > 1; W /= (W < kBisectSplit ? W : kBisectSplit)) st.kernel_launches += 2;
     }

@@ -54,9 +54,10 @@ struct DevBatch {
 };
 
 constexpr int kWaitPolls = 1 << 22;       // default bound of the TMA scan's mbarrier waits
-// persistent grid of the lane-per-level kernels: CTAs per SM launched (4 fit
-// at their register use; fewer leave room for the CTA-per-level branch that
-// runs beside them)
+// persistent grid of the lane-per-level kernels (refine32, newton_df,
+// norm_df): threads per CTA and CTAs per SM launched (together 512 threads at
+// up to 128 registers, the whole register file)
+constexpr int kLaneThreads = 128;
 constexpr int kLaneCtasPerSm = 4;
 constexpr int kRefineMaxIter = 48;        // default cap on a level's FP32 refinement passes
 __device__ __forceinline__ int refine_cap(const DevBatch& b) { return b.max_iter > 0 ? b.max_iter : kRefineMaxIter; }

@@ -64,8 +64,11 @@ namespace epscu {
 
 namespace {
 
+// CTA shape of the group passes: threads per CTA and the persistent grid's
+// CTAs per SM
 constexpr int kLongThreads = 256;
 constexpr int kLongWarps = kLongThreads / 32;
+constexpr int kLongCtasPerSm = 2;
 
 // [[a, b], [c, d]] 2^e acting on the column (A, D)
 struct Mat2 {
@@ -1007,7 +1010,7 @@ __device__ __forceinline__ bool grp_cancelled(const Grp<NW>& G, const DevBatch& 
 constexpr double kTol32Long = 2e-9;
 
 template <int NW>
-__global__ void __launch_bounds__(kLongThreads) refine_long_kernel(DevBatch b, int mode, const int32_t* list,
+__global__ void __launch_bounds__(kLongThreads, kLongCtasPerSm) refine_long_kernel(DevBatch b, int mode, const int32_t* list,
                                                                    const int32_t* list_len, int qid) {
     constexpr int kG = kLongThreads / (32 * NW);
     __shared__ SharedDF<NW> shd[kG];
@@ -1173,7 +1176,7 @@ __global__ void __launch_bounds__(kLongThreads) refine_long_kernel(DevBatch b, i
 // psi-hat in the level's row (MODE 3) and the last pass is the one kept;
 // scale_psi applies the constants afterwards.
 template <int NW>
-__global__ void __launch_bounds__(kLongThreads) norm_long_kernel(DevBatch b, const int32_t* list,
+__global__ void __launch_bounds__(kLongThreads, kLongCtasPerSm) norm_long_kernel(DevBatch b, const int32_t* list,
                                                                  const int32_t* list_len, int qid) {
     constexpr int kG = kLongThreads / (32 * NW);
     __shared__ SharedDF<NW> shd[kG];
@@ -1238,7 +1241,7 @@ __global__ void __launch_bounds__(kLongThreads) norm_long_kernel(DevBatch b, con
 // final pass stores the unnormalised psi-hat in the level's row (scale_psi
 // applies the constants).  The level joins the long list, so the adjoint's
 // recompute path (write_long) writes its psi.  One CTA per level.
-__global__ void __launch_bounds__(kLongThreads) twist_long_kernel(DevBatch b) {
+__global__ void __launch_bounds__(kLongThreads, kLongCtasPerSm) twist_long_kernel(DevBatch b) {
     __shared__ SharedDF<kLongWarps> sh;
     const Grp<kLongWarps> G;
     const int n = min(b.hdr->n_twist, b.max_twist);
@@ -1291,7 +1294,7 @@ __global__ void __launch_bounds__(kLongThreads) twist_long_kernel(DevBatch b) {
 // psi of the listed levels in FP64 from the final constants (window points
 // and psi_k; the rest of each row is zero): the adjoint's recompute path.
 // One CTA per level.
-__global__ void __launch_bounds__(kLongThreads) write_long_kernel(DevBatch b, const int32_t* list,
+__global__ void __launch_bounds__(kLongThreads, kLongCtasPerSm) write_long_kernel(DevBatch b, const int32_t* list,
                                                                   const int32_t* list_len) {
     __shared__ SharedDF<kLongWarps> sh;
     const Grp<kLongWarps> G;
@@ -1318,25 +1321,25 @@ __global__ void __launch_bounds__(kLongThreads) write_long_kernel(DevBatch b, co
 void launch_refine_long(const DevBatch& b, int sm_count, cudaStream_t s) {
     if (!b.long_list) return;
     refine_long_kernel<kLongWarps>
-        <<<sm_count * 2, kLongThreads, 0, s>>>(b, 0, b.long_list, &b.hdr->n_long, kQLongRefine);
+        <<<sm_count * kLongCtasPerSm, kLongThreads, 0, s>>>(b, 0, b.long_list, &b.hdr->n_long, kQLongRefine);
 }
 void launch_fallback_long(const DevBatch& b, int sm_count, cudaStream_t s) {
     if (!b.fallback_list) return;
     refine_long_kernel<kLongWarps>
-        <<<sm_count * 2, kLongThreads, 0, s>>>(b, 1, b.fallback_list, &b.hdr->fallbacks, kQFallback);
+        <<<sm_count * kLongCtasPerSm, kLongThreads, 0, s>>>(b, 1, b.fallback_list, &b.hdr->fallbacks, kQFallback);
 }
 void launch_norm_long(const DevBatch& b, int sm_count, cudaStream_t s) {
     if (!b.long_list) return;
-    norm_long_kernel<kLongWarps><<<sm_count * 2, kLongThreads, 0, s>>>(b, b.long_list, &b.hdr->n_long, kQNormLong);
+    norm_long_kernel<kLongWarps><<<sm_count * kLongCtasPerSm, kLongThreads, 0, s>>>(b, b.long_list, &b.hdr->n_long, kQNormLong);
 }
 void launch_twist_long(const DevBatch& b, int sm_count, cudaStream_t s) {
     if (!b.twist_list || !b.long_list) return;
-    twist_long_kernel<<<sm_count * 2, kLongThreads, 0, s>>>(b);
+    twist_long_kernel<<<sm_count * kLongCtasPerSm, kLongThreads, 0, s>>>(b);
 }
 void launch_write_long(const DevBatch& b, int sm_count, cudaStream_t s) {
     // the group levels of both tiers (the recompute path: one CTA per level)
-    if (b.long_list) write_long_kernel<<<sm_count * 2, kLongThreads, 0, s>>>(b, b.long_list, &b.hdr->n_long);
-    if (b.mid_list) write_long_kernel<<<sm_count * 2, kLongThreads, 0, s>>>(b, b.mid_list, &b.hdr->n_mid);
+    if (b.long_list) write_long_kernel<<<sm_count * kLongCtasPerSm, kLongThreads, 0, s>>>(b, b.long_list, &b.hdr->n_long);
+    if (b.mid_list) write_long_kernel<<<sm_count * kLongCtasPerSm, kLongThreads, 0, s>>>(b, b.mid_list, &b.hdr->n_mid);
 }
 // the middle tier is in use (its list can be non-empty): the same threshold
 // as the window kernel's
@@ -1345,11 +1348,11 @@ static bool mid_tier_on(const DevBatch& b) {
 }
 void launch_refine_mid(const DevBatch& b, int sm_count, cudaStream_t s) {
     if (!mid_tier_on(b)) return;
-    refine_long_kernel<1><<<sm_count * 2, kLongThreads, 0, s>>>(b, 2, b.mid_list, &b.hdr->n_mid, kQMidRefine);
+    refine_long_kernel<1><<<sm_count * kLongCtasPerSm, kLongThreads, 0, s>>>(b, 2, b.mid_list, &b.hdr->n_mid, kQMidRefine);
 }
 void launch_norm_mid(const DevBatch& b, int sm_count, cudaStream_t s) {
     if (!mid_tier_on(b)) return;
-    norm_long_kernel<1><<<sm_count * 2, kLongThreads, 0, s>>>(b, b.mid_list, &b.hdr->n_mid, kQNormMid);
+    norm_long_kernel<1><<<sm_count * kLongCtasPerSm, kLongThreads, 0, s>>>(b, b.mid_list, &b.hdr->n_mid, kQNormMid);
 }
 
 }  // namespace epscu

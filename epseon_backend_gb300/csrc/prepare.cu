@@ -319,6 +319,7 @@ __global__ void bracket_kernel(DevBatch b) {
     for (int s = threadIdx.x; s < m.n_out; s += blockDim.x) {
         const int v = b.min_level + s;
         int lo = 0, hi = m.n_trial;
+        int top = -1;  // trial index of the bracket's upper end (lo when -1)
         if (!b.bis_list) {
             while (lo < hi) {
                 const int mid = lo + (hi - lo) / 2;
@@ -341,12 +342,19 @@ __global__ void bracket_kernel(DevBatch b) {
                     if (c[min(km * kBisectCoarse - 1, last)] > v) kh = km;
                     else kl = km + 1;
                 }
+                // then down the cell's halves while their midpoints have a
+                // count (a cell cut into fewer parts ends the descent early:
+                // the bracket is the last cell (a, a + W])
                 int a = (kl - 1) * kBisectCoarse - 1;
-                for (int W = kBisectCoarse; W > 1; W >>= 1) {
+                int W = kBisectCoarse;
+                for (; W > 1; W >>= 1) {
                     const int mid = a + W / 2;
-                    if ((mid >= last ? ctop : c[mid]) <= v) a = mid;
+                    const int cm = mid >= last ? ctop : c[mid];
+                    if (cm < 0) break;  // no count taken there
+                    if (cm <= v) a = mid;
                 }
                 lo = min(a + 1, last);
+                top = min(a + W, last);
             }
         }
         LevelWork w;
@@ -364,10 +372,11 @@ __global__ void bracket_kernel(DevBatch b) {
             w.status |= EPSCU_STATUS_NOTFOUND;
             w.lo = w.hi = w.E = m.e_cap;
         } else {
+            if (top < lo) top = lo;
             w.lo = lo == 0 ? m.e_lo : trial_energy(m, lo - 1);
-            w.hi = trial_energy(m, lo);
+            w.hi = trial_energy(m, top);
             w.E = __dmul_rn(0.5, __dadd_rn(w.lo, w.hi));
-            w.n_in_bracket = c[lo] - (lo == 0 ? 0 : c[lo - 1]);
+            w.n_in_bracket = c[top] - (lo == 0 ? 0 : c[lo - 1]);
         }
         w.lo0 = w.lo;
         w.hi0 = w.hi;

@@ -455,9 +455,11 @@ __global__ void __launch_bounds__(256) bisect_plan_kernel(DevBatch b, int W, int
                 const int a = t * W - 1;  // cell (a, a + W], count(-1) = 0
                 const int ca = a < 0 ? 0 : c[a];
                 const int cb = c[min(a + W, last)];
+                // a coarse cell with one level is cut into kBisectSingle parts
+                const int parts = (cb - ca == 1 && W == kBisectCoarse) ? min(kBisectSingle, split) : split;
                 if (ca >= 0 && cb > ca)
-                    for (int q = 1; q < split; ++q) {
-                        const int pt = a + q * (W / split);
+                    for (int q = 1; q < parts; ++q) {
+                        const int pt = a + q * (W / parts);
                         if (pt < last) list[atomicAdd(&s_n, 1)] = pt;
                     }
             }
@@ -699,9 +701,14 @@ void launch_bisect_scan(const DevBatch& b, const ScanShape& sh, int sm_count, cu
     // one.  Every round lasts about one march of its longest window (the
     // total work of a round is a fraction of that), so fewer rounds with more
     // counts each are shorter: the scan stage went from 6.8 to 5.6 ms (two
-    // rounds) and 5.2 ms (one) on the 2048-potential batch.  The brackets are
-    // the same, and so is the bracket kernel's descent (every midpoint it
-    // visits has a count)
+    // rounds) and 5.2 ms (one) on the 2048-potential batch.  A coarse cell
+    // that holds one level is only halved (kBisectSingle): its bracket of four
+    // spacings isolates the level already, the round takes one count for it
+    // instead of seven, and the refinement needs about one pass more.
+    // Measured on the same batch (scan stage / step): 5.00 / 31.6 ms with
+    // seven counts, 4.23 / 30.6 with three, 3.90 / 30.4 with one, 3.29 / 30.7
+    // with none (the whole cell as the bracket).  The bracket kernel descends
+    // while the midpoints it visits have a count.
     for (int W = kBisectCoarse; W > 1;) {
         const int split = W < kBisectSplit ? W : kBisectSplit;
         cudaMemsetAsync(&b.hdr->bis_items_n, 0, 2 * sizeof(int32_t), s);  // the round's items and queue
