@@ -163,16 +163,16 @@ __device__ __forceinline__ int match_index(const PotMeta& m, const double* __res
 }
 
 // bisection scan: the throughput scan on every kBisectCoarse-th trial
-// energy, then cells halved round by round
-constexpr int kBisectCoarse = 8;
-// points per cell and round of the bisection scan's rounds (a power of two
-// dividing kBisectCoarse)
-constexpr int kBisectSplit = 8;
+// energy, then counts inside the coarse cells whose end counts differ
+constexpr int kBisectCoarse = 16;
+// parts a cell with two or more levels is cut into per round (a power of two
+// dividing kBisectCoarse; equal to it: one round, a count at every trial
+// energy of the cell)
+constexpr int kBisectSplit = 16;
 // parts a coarse cell that holds exactly one level is cut into (a power of
 // two dividing kBisectCoarse; 1: no count inside, the level's bracket is the
-// whole cell, which isolates it already).  Cells with two or more levels are
-// cut into kBisectSplit parts round by round.
-constexpr int kBisectSingle = 2;
+// whole cell, which isolates it already)
+constexpr int kBisectSingle = 4;
 // batches of at least this many potentials take the bisection scan (smaller
 // ones have too few CTAs per round to cover its latency; measured on GB300)
 constexpr int kBisectMinPotentials = 512;

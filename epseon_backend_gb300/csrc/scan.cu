@@ -421,17 +421,19 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
 
 // ------------------------------------------------------------ bisection scan
 // The levels' brackets need the count only where it changes: the counts at
-// every kBisectCoarse-th trial energy (and the last), then, round by round,
-// at the midpoint of every cell whose end counts differ, until those cells
-// are one trial spacing wide.  That is the bracket the full scan gives (the
-// count is monotone in the energy), from ~128 + 6 (levels) counts per
-// potential instead of n_trial.  counts[] holds -1 where no count was taken.
+// every kBisectCoarse-th trial energy (and the last), then counts inside the
+// cells whose end counts differ.  A cell with two or more levels is cut to
+// single trial spacings (the full scan's brackets there: the count is
+// monotone in the energy); a cell with one level into kBisectSingle parts,
+// whose bracket isolates the level.  counts[] holds -1 where no count was
+// taken.
 
 // The trial indices of the next round (W = 0: the coarse boundaries; else
 // the split - 1 interior points that cut each cell of width W whose end counts
-// differ into `split` equal cells; split = 2 is bisection), and the
-// round's work items: the potential's list in chunks of kCountEnergies, so
-// that the count kernel runs every chunk of every potential side by side.
+// differ into `split` equal cells, or kBisectSingle - 1 points for a coarse
+// cell with one level), and the round's work items: the potential's list in
+// chunks of kCountEnergies, so that the count kernel runs every chunk of
+// every potential side by side.
 // One CTA per potential, longest grids first (their items are listed first).
 constexpr int kCountThreads = 128;
 constexpr int kCountEnergies = kCountThreads / 2;
@@ -695,20 +697,19 @@ void launch_bisect_scan(const DevBatch& b, const ScanShape& sh, int sm_count, cu
     cudaMemsetAsync(b.counts, 0xff, sizeof(int32_t) * (size_t)b.n * b.n_trial, s);  // -1: no count taken
     // the coarse grid with the throughput scan, then the bisection rounds
     launch_scan32(b, sh, sm_count, s, kBisectCoarse);
-    // each round cuts the cells that hold a level into kBisectSplit parts
-    // (the last round into what is left): with cells of 8 trial spacings and
-    // a split of 8, one round of 7 points per cell instead of three rounds of
-    // one.  Every round lasts about one march of its longest window (the
-    // total work of a round is a fraction of that), so fewer rounds with more
-    // counts each are shorter: the scan stage went from 6.8 to 5.6 ms (two
-    // rounds) and 5.2 ms (one) on the 2048-potential batch.  A coarse cell
-    // that holds one level is only halved (kBisectSingle): its bracket of four
-    // spacings isolates the level already, the round takes one count for it
-    // instead of seven, and the refinement needs about one pass more.
-    // Measured on the same batch (scan stage / step): 5.00 / 31.6 ms with
-    // seven counts, 4.23 / 30.6 with three, 3.90 / 30.4 with one, 3.29 / 30.7
-    // with none (the whole cell as the bracket).  The bracket kernel descends
-    // while the midpoints it visits have a count.
+    // each round cuts the cells that hold two or more levels into
+    // kBisectSplit parts (the last round into what is left), and a cell that
+    // holds one level into kBisectSingle parts once: its bracket of
+    // kBisectCoarse / kBisectSingle spacings isolates the level already, and
+    // the refinement needs about one pass more than from one spacing.  Every
+    // round lasts about one march of its longest window (the total work of a
+    // round is a fraction of that), so fewer rounds with more counts each are
+    // shorter.  Measured on the 2048-potential batch (scan stage / step):
+    // cells of 8, three rounds of 2: 6.8 ms (scan); cells of 8, one round of
+    // 8: 5.0 / 31.6 ms; one-level cells halved: 3.9 / 30.4 ms; cells of 16
+    // (15 counts in a cell with several levels, 3 in a one-level cell):
+    // 3.6 / 29.7 ms; cells of 32 (31 and 7): 4.9 / 30.8 ms.  The bracket
+    // kernel descends while the midpoints it visits have a count.
     for (int W = kBisectCoarse; W > 1;) {
         const int split = W < kBisectSplit ? W : kBisectSplit;
         cudaMemsetAsync(&b.hdr->bis_items_n, 0, 2 * sizeof(int32_t), s);  // the round's items and queue

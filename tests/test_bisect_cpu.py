@@ -18,9 +18,9 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-COARSE = 8  # kBisectCoarse
-SPLIT = 8   # kBisectSplit
-SINGLE = 2  # kBisectSingle
+COARSE = 16  # kBisectCoarse
+SPLIT = 16  # kBisectSplit
+SINGLE = 4  # kBisectSingle
 
 
 def rounds(full: np.ndarray, single: int = SINGLE) -> np.ndarray:
@@ -107,7 +107,7 @@ def check_brackets(full: np.ndarray, c: np.ndarray, single: int = SINGLE) -> Non
 
 @pytest.mark.parametrize("n_trial", [1, 2, 7, 8, 9, 63, 64, 65, 1000, 1024, 8191, 8192])
 @pytest.mark.parametrize("seed", [0, 1, 2])
-@pytest.mark.parametrize("single", [1, 2, 4, 8])
+@pytest.mark.parametrize("single", [1, 2, 4, 8, 16])
 def test_descent_brackets_every_level(n_trial, seed, single):
     rng = np.random.default_rng(seed + 31 * n_trial)
     n_levels = int(rng.integers(0, 3 * n_trial // 2 + 3))
