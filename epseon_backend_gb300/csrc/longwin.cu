@@ -41,7 +41,7 @@
 // Kernels (one group per level, levels taken from a device queue over a list
 // the window kernel fills; the lane-per-level kernels skip these levels):
 //   refine_long : from the scan bracket, FP32 passes (the same three phases
-//                 in FP32, long_side32) to 2e-9, then double-float
+//                 in FP32, long_side32) to a Newton step of 3e-8, then double-float
 //                 state-only Newton to 1e-12 (replaces refine32 + newton_df);
 //                 run again over the levels newton_df could not settle (the
 //                 fallback: any window length, full double-float passes from
@@ -988,8 +988,10 @@ __device__ __forceinline__ bool grp_cancelled(const Grp<NW>& G, const DevBatch& 
 }
 
 // Levels on groups of warps, in up to three stages:
-//   1. FP32 passes (long_pass32): safeguarded Cooley-Newton to |dE| <= 2e-9
-//      with the count bracket, the match point moved to the peak of |psi|;
+//   1. FP32 passes (long_pass32): safeguarded Cooley-Newton with the count
+//      bracket, the match point moved to the peak of |psi|, until a Newton
+//      step of at most kTol32Long is taken (the energy after it is then far
+//      inside stage 2's first-pass acceptance);
 //   2. double-float state-only passes with the FP32 sum as the Newton
 //      denominator (as newton_df): usually one step, accepted from within
 //      1e-8 (the chunked FP32 sum is accurate to ~1e-6);
@@ -1007,7 +1009,10 @@ __device__ __forceinline__ bool grp_cancelled(const Grp<NW>& G, const DevBatch& 
 // newton_df's acceptance rule, then stage 3 if it does not settle).  Every
 // thread of a group runs the same control flow on the leader's pass results
 // (the group's passes are collective).
-constexpr double kTol32Long = 2e-9;
+// (Measured on the 2048-potential batch, refine_long / step: 2e-9 7.8 /
+// 30.0 ms, 1e-8 7.4 / 29.8, 3e-8 7.4 / 29.6, 1e-7 7.0 / 29.6 with more
+// double-float passes after it.)
+constexpr double kTol32Long = 3e-8;
 
 template <int NW>
 __global__ void __launch_bounds__(kLongThreads, kLongCtasPerSm) refine_long_kernel(DevBatch b, int mode, const int32_t* list,
