@@ -153,6 +153,13 @@ __device__ __forceinline__ Pass32 cooley32(const PotMeta& m, const float2* __res
 // alone and the pass saw its node count; otherwise it is confirmed by a count
 // on the far side of the predicted root, or the level continues by bisection.
 constexpr double kTol32 = 2e-9;
+// a Newton step accepted outright (the level alone in its scan bracket, its
+// node count seen): the energy after it is within ~1e-4 of the step (the
+// relative error of the FP32 sum) plus the step's square over the curvature.
+// (Measured on the 2048-potential batch: 2e-8 takes no fewer passes, the
+// quadratic steps jump past it; 5e-8 and above leave more norm passes to
+// redo, +0.6 and +2.6 ms a step.)
+constexpr double kAccept32 = 2e-9;
 
 // The FP32 refinement of the level in slot `slot` (one lane); false when the
 // level takes no lane refinement (no bracket, a long window, or cancelled).
@@ -209,15 +216,15 @@ __device__ __forceinline__ bool refine32_level(const DevBatch& b, int slot) {
             En = E + r.dE;
             if (!(En > lo && En < hi) || !isfinite(En)) {
                 En = 0.5 * (lo + hi);
+            } else if (fabs(r.dE) <= kAccept32 && w.n_in_bracket == 1 && r.nodes == w.v) {
+                // the scan bracket holds this level alone and the pass sees
+                // its node count: the root is the level (the double-float
+                // Newton re-checks the count)
+                E_star = En;
+                done = true;
+                break;
             } else if (fabs(r.dE) <= kTol32) {
                 E_star = En;
-                if (w.n_in_bracket == 1 && r.nodes == w.v) {
-                    // the scan bracket holds this level alone and the pass
-                    // sees its node count: the root is the level (the
-                    // double-float Newton re-checks the count)
-                    done = true;
-                    break;
-                }
                 En = En + (r.dE >= 0.0 ? kTol32 : -kTol32);
                 if (En <= lo || En >= hi) En = 0.5 * (E_star + (r.dE >= 0.0 ? hi : lo));
                 confirming = true;
