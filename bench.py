@@ -453,7 +453,7 @@ def main():
     # the scan stage in the same unit (the coarse scan32 launch plus, on large
     # batches, the bisection rounds; scan32 alone is FP32-issue-bound)
     scan_ach = 9.0 * st.scan_point_updates / (st.ms_scan * 1e-3) / 1e12
-    roof_scan = {"kernel": "scan stage (scan32_kernel" + (" on every 8th trial energy + bisection rounds)"
+    roof_scan = {"kernel": "scan stage (scan32_kernel" + (" on every 16th trial energy + the bisection count round)"
                                                           if len(b) >= 512 else ")"),
                  "achieved": scan_ach, "peak": fp32_peak, "unit": "TFLOP/s", "frac": scan_ach / fp32_peak,
                  "ms": st.ms_scan, "point_updates": int(st.scan_point_updates),
