@@ -71,7 +71,7 @@ struct Header {
     int32_t fallbacks;      // levels that needed the bisection fallback
     int32_t n_units;        // warp work units (<= 32 levels of one potential)
     int32_t n_twist;        // levels handed to the twist-index search
-    int32_t queue[14];      // work-queue heads of the per-level kernels
+    int32_t queue[16];      // work-queue heads of the per-level kernels
     int32_t n_long;         // levels whose window takes the CTA-per-level passes
     int32_t n_mid;          // levels whose window takes the warp-per-level passes
     int32_t pad_mid;
@@ -94,10 +94,12 @@ struct Header {
 
 // queue ids of the per-level kernels
 enum { kQRefine32 = 0, kQNewtonDF, kQNormDF, kQWriteDF, kQBisect64, kQNorm64, kQWrite64, kQLongRefine, kQFallback,
-       kQNormLong, kQTwistLong, kQMidRefine, kQNormMid, kQScalePsi };
+       kQNormLong, kQTwistLong, kQMidRefine, kQNormMid, kQScalePsi, kQNormFallback };
 
 // internal level flags (not reported: gather keeps the public bits only)
-// the Newton stage handed the level to the fallback
+// the Newton stage handed the level to the fallback: its refinement, norm pass
+// and (recompute) write run one CTA per level over the fallback list, and its
+// norm constants are the group passes' (the lane kernels skip it)
 #define EPSCU_STATUS_FALLBACK 0x10000
 // the level's passes run one CTA per level (longwin.cu)
 #define EPSCU_STATUS_LONG 0x20000

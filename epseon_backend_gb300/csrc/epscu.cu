@@ -12,8 +12,9 @@
 //   inside the cells where the counts change) -> level set-up + brackets
 //   plain : bisect64 -> norm64 -> twist64 -> write64            (native FP64)
 //   fast  : window, then two branches on two streams (graph fork/join):
-//             lane levels: refine32 -> newton_df -> fallback -> norm_df
-//             long levels: refine_long -> norm_long -> zero_psi
+//             lane levels: refine32 -> newton_df -> norm_df
+//             long levels: refine_long -> norm_long, then (after newton_df)
+//                          the fallback levels' refinement and norm -> zero_psi
 //           -> twist_long -> scale_psi   (FP32, then compensated FP32 with
 //           FP64 matching and norm integral; the norm passes store psi-hat)
 //   -> gather into the caller's layout.
@@ -71,7 +72,7 @@ struct epscu_ctx {
     int sm_count = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;  // the long levels' branch of the fast pipeline
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_newton = nullptr;
     size_t block = size_t(64) << 20;
     std::map<std::string, DevBuf> bufs;
     std::map<std::string, std::pair<void*, size_t>> pinned;
@@ -108,6 +109,7 @@ struct epscu_ctx {
         if (ev_out) cudaEventDestroy(ev_out);
         if (ev_fork) cudaEventDestroy(ev_fork);
         if (ev_join) cudaEventDestroy(ev_join);
+        if (ev_newton) cudaEventDestroy(ev_newton);
         if (stream2) cudaStreamDestroy(stream2);
         if (stream) cudaStreamDestroy(stream);
     }
@@ -237,6 +239,7 @@ epscu_status epscu_create(int32_t device_ordinal, epscu_ctx** out) {
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_out, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_newton, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         delete c;
         return fail(EPSCU_ERR_CUDA, std::string("context set-up: ") + cudaGetErrorString(e));
@@ -336,17 +339,23 @@ void enqueue_pipeline(epscu_ctx* ctx, const DevBatch& b, int method, bool want_p
             // stream beside the compute-bound lane kernels (the norm passes
             // write only inside the windows, so they need not wait for it;
             // zeroing first held back the long levels' refinement: measured
-            // 29.6 against 28.7 ms a step on the 2048-potential batch)
+            // 29.6 against 28.7 ms a step on the 2048-potential batch).  The
+            // levels newton_df could not settle take their refinement and
+            // norm pass on CTAs in that branch too, once newton_df is done,
+            // so norm_df need not wait for them (28.7 -> 27.7 ms)
             cudaEventRecord(ctx->ev_fork, s);
             cudaStreamWaitEvent(ctx->stream2, ctx->ev_fork, 0);
             launch_refine32(b, ctx->sm_count, s);
             launch_refine_long(b, ctx->sm_count, ctx->stream2);
             launch_norm_long(b, ctx->sm_count, ctx->stream2);
-            if (want_psi) launch_zero_psi(b, ctx->sm_count, ctx->stream2);
-            cudaEventRecord(ctx->ev_join, ctx->stream2);
             launch_refine_mid(b, ctx->sm_count, s);
             launch_newton_df(b, ctx->sm_count, s);
-            launch_fallback_long(b, ctx->sm_count, s);
+            cudaEventRecord(ctx->ev_newton, s);
+            cudaStreamWaitEvent(ctx->stream2, ctx->ev_newton, 0);
+            launch_fallback_long(b, ctx->sm_count, ctx->stream2);
+            launch_norm_fallback(b, ctx->sm_count, ctx->stream2);
+            if (want_psi) launch_zero_psi(b, ctx->sm_count, ctx->stream2);
+            cudaEventRecord(ctx->ev_join, ctx->stream2);
             launch_norm_mid(b, ctx->sm_count, s);
             launch_norm_df(b, ctx->sm_count, s);
             cudaStreamWaitEvent(s, ctx->ev_join, 0);
@@ -361,6 +370,7 @@ void enqueue_pipeline(epscu_ctx* ctx, const DevBatch& b, int method, bool want_p
             launch_refine_mid(b, ctx->sm_count, s);
             launch_newton_df(b, ctx->sm_count, s);
             launch_fallback_long(b, ctx->sm_count, s);
+            launch_norm_fallback(b, ctx->sm_count, s);
             rec(10);
             if (want_psi) launch_zero_psi(b, ctx->sm_count, s);
             rec(11);
@@ -768,11 +778,12 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     // plain: prepare, scan64, level/unit setup, bracket, bisect64, norm64,
     // twist64, gather (+ write64); fast: prepare, scan window, scan32, level/unit
     // setup, bracket, window, refine32, refine_long, newton_df, fallback
-    // (refine_long over the fallback list), norm_df, norm_long, twist_long,
-    // gather (+ refine_mid, norm_mid with the middle tier; + zero_psi, scale_psi)
+    // (refine_long over the fallback list), its norm (norm_long over the
+    // fallback list), norm_df, norm_long, twist_long, gather (+ refine_mid,
+    // norm_mid with the middle tier; + zero_psi, scale_psi)
     const bool psi_kernels = psi_on;
     const bool mid_on = b.mid_list && (b.mid_window != 0 ? b.mid_window : kMidWindow) > 0;
-    st.kernel_launches = method == EPSCU_METHOD_FAST_FP32C ? 15 + (mid_on ? 2 : 0) + (psi_kernels ? 2 : 0)
+    st.kernel_launches = method == EPSCU_METHOD_FAST_FP32C ? 16 + (mid_on ? 2 : 0) + (psi_kernels ? 2 : 0)
                                                            : 9 + (psi_kernels ? 1 : 0);
     if (b.bis_list) {  // the plan + count rounds after the coarse scan32
         for (int W = kBisectCoarse; W > 1; W /= (W < kBisectSplit ? W : kBisectSplit)) st.kernel_launches += 2;

@@ -267,10 +267,12 @@ __device__ __forceinline__ bool newton_df_level(const DevBatch& b, int slot) {
 // The norm pass of the level in slot `slot` and its match-point candidates:
 // sums, node count, peak of |psi| and the constants of the write; with psi
 // requested every pass also stores the unnormalised psi-hat in the level's
-// row.  False when the level takes no lane norm.
+// row.  False when the level takes no lane norm (a group level, or one the
+// fallback refined: norm_long normalises it over the fallback list).
 __device__ __forceinline__ bool norm_df_level(const DevBatch& b, int slot) {
     LevelWork w = b.levels[slot];
-    if ((w.status & (EPSCU_STATUS_NOTFOUND | EPSCU_STATUS_CANCELLED)) || is_long(w)) return false;
+    if ((w.status & (EPSCU_STATUS_NOTFOUND | EPSCU_STATUS_CANCELLED | EPSCU_STATUS_FALLBACK)) || is_long(w))
+        return false;
     const PotMeta m = b.meta[w.p];
     const float2* Wf = b.Wf2 + m.offf;
     const double* W = b.W64 + m.off;

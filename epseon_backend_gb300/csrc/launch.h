@@ -130,6 +130,7 @@ void launch_fallback_long(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_norm_long(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_write_long(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_twist_long(const DevBatch& b, int sm_count, cudaStream_t s);
+void launch_norm_fallback(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_refine_mid(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_norm_mid(const DevBatch& b, int sm_count, cudaStream_t s);
 

@@ -48,9 +48,11 @@
 //                 the scan bracket widened by one trial spacing), and over
 //                 the middle list from the lane FP32 refinement's result;
 //   norm_long   : the norm pass and its match-point candidates (as norm_df),
-//                 storing psi-hat as tagged float pairs for scale_psi;
+//                 storing psi-hat as tagged float pairs for scale_psi; run
+//                 over the long list and over the fallback list;
 //   twist_long  : the twist-index search for the levels the norm passes flag;
-//   write_long  : psi from the final constants (the adjoint's recompute path).
+//   write_long  : psi from the final constants (the adjoint's recompute path;
+//                 the long, middle and fallback lists).
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -1157,7 +1159,6 @@ __global__ void __launch_bounds__(kLongThreads, kLongCtasPerSm) refine_long_kern
         }
         if (G.leader()) {
             if (!done) w.status |= EPSCU_STATUS_MAXITER;
-            w.status &= ~EPSCU_STATUS_FALLBACK;
             w.lo = lo;
             w.hi = hi;
             w.E = E;
@@ -1337,6 +1338,11 @@ void launch_norm_long(const DevBatch& b, int sm_count, cudaStream_t s) {
     if (!b.long_list) return;
     norm_long_kernel<kLongWarps><<<sm_count * kLongCtasPerSm, kLongThreads, 0, s>>>(b, b.long_list, &b.hdr->n_long, kQNormLong);
 }
+void launch_norm_fallback(const DevBatch& b, int sm_count, cudaStream_t s) {
+    if (!b.fallback_list) return;
+    norm_long_kernel<kLongWarps>
+        <<<sm_count * kLongCtasPerSm, kLongThreads, 0, s>>>(b, b.fallback_list, &b.hdr->fallbacks, kQNormFallback);
+}
 void launch_twist_long(const DevBatch& b, int sm_count, cudaStream_t s) {
     if (!b.twist_list || !b.long_list) return;
     twist_long_kernel<<<sm_count * kLongCtasPerSm, kLongThreads, 0, s>>>(b);
@@ -1345,6 +1351,8 @@ void launch_write_long(const DevBatch& b, int sm_count, cudaStream_t s) {
     // the group levels of both tiers (the recompute path: one CTA per level)
     if (b.long_list) write_long_kernel<<<sm_count * kLongCtasPerSm, kLongThreads, 0, s>>>(b, b.long_list, &b.hdr->n_long);
     if (b.mid_list) write_long_kernel<<<sm_count * kLongCtasPerSm, kLongThreads, 0, s>>>(b, b.mid_list, &b.hdr->n_mid);
+    if (b.fallback_list)
+        write_long_kernel<<<sm_count * kLongCtasPerSm, kLongThreads, 0, s>>>(b, b.fallback_list, &b.hdr->fallbacks);
 }
 // the middle tier is in use (its list can be non-empty): the same threshold
 // as the window kernel's

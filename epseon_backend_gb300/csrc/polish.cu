@@ -6,7 +6,8 @@
 //
 //  newton_df : Cooley corrections from the FP32 energy (one or two passes) in
 //              an FP64 count bracket; levels that do not settle go to the
-//              CTA-per-level Newton of longwin.cu (the fallback).
+//              CTA-per-level Newton of longwin.cu (the fallback), which also
+//              takes their norm and write passes.
 //  norm_df   : sums, node count, peak of |psi| and the constants of the
 //              write; with psi requested its final pass also stores the
 //              unnormalised psi-hat in the level's row as tagged float pairs
@@ -74,7 +75,7 @@ __global__ void __launch_bounds__(kThreads, 4) write_df_kernel(DevBatch b) {
         if (lane >= unit.y) continue;
         const int slot = unit.x + lane;
         const LevelWork w = b.levels[slot];
-        if (no_result(w) || is_long(w)) continue;
+        if (no_result(w) || is_long(w) || (w.status & EPSCU_STATUS_FALLBACK)) continue;
         const PotMeta m = b.meta[w.p];
         double* out = b.psi + m.psi_off + (int64_t)(w.v - b.min_level) * m.N;
         const float2* Wf = b.Wf2 + m.offf;
