@@ -32,16 +32,28 @@ namespace {
 // thread: the kernel is bound by HBM latency otherwise).
 constexpr int kAdjTile = 256;  // levels staged per round
 
-__global__ void __launch_bounds__(256) adjoint_kernel(DevBatch b, const double* __restrict__ gE, double* __restrict__ gV,
-                                                      const int64_t* __restrict__ offsets, const double* __restrict__ psi,
-                                                      int accumulate) {
-    __shared__ int s_lo, s_hi;
+__global__ void __launch_bounds__(kAdjointPoints) adjoint_kernel(DevBatch b, const double* __restrict__ gE,
+                                                                 double* __restrict__ gV,
+                                                                 const int64_t* __restrict__ offsets,
+                                                                 const int32_t* __restrict__ tiles,
+                                                                 const double* __restrict__ psi, int accumulate) {
+    __shared__ int s_lo, s_hi, s_p;
     __shared__ int2 s_win[kAdjTile];
     __shared__ float s_gh[kAdjTile], s_gl[kAdjTile];  // dL/dE as double-float pairs
-    const int p = blockIdx.y;
+    if (threadIdx.x == 0) {
+        // the potential of this tile: the last p with tiles[p] <= blockIdx.x
+        int lo = 0, hi = b.n - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (tiles[mid] <= (int)blockIdx.x) lo = mid;
+            else hi = mid - 1;
+        }
+        s_p = lo;
+    }
+    __syncthreads();
+    const int p = s_p;
     const PotMeta m = b.meta[p];
-    const int i_a = blockIdx.x * blockDim.x;
-    if (i_a >= m.N) return;
+    const int i_a = ((int)blockIdx.x - tiles[p]) * kAdjointPoints;
     const int i_b = min(i_a + (int)blockDim.x, m.N) - 1;
     const LevelWork* lw = b.levels + m.level_base;
     if (threadIdx.x == 0) {
@@ -129,14 +141,12 @@ void launch_adjoint_explicit(int32_t n, int32_t cap, int32_t max_N, const int64_
     adjoint_explicit_kernel<<<grid, 256, 0, s>>>(cap, offsets, N, h, n_out, psi_off, psi, gE, gV);
 }
 
-void launch_adjoint(const DevBatch& b, const double* dL_dE, double* dL_dV, int64_t total_points,
-                    const int64_t* offsets_dev, int recompute, int sm_count, cudaStream_t s) {
-    (void)total_points;
-    (void)recompute;
-    (void)sm_count;
-    // grid.x covers the longest grid; threads past a shorter grid exit at once
-    dim3 grid((b.max_N + 255) / 256, b.n);
-    adjoint_kernel<<<grid, 256, 0, s>>>(b, dL_dE, dL_dV, offsets_dev, b.psi, 0);
+void launch_adjoint(const DevBatch& b, const double* dL_dE, double* dL_dV, const int64_t* offsets_dev,
+                    const int32_t* tiles_dev, int32_t n_tiles, cudaStream_t s) {
+    // one CTA per tile of kAdjointPoints points of a potential (a 2-D grid
+    // over the longest grid left ~3/4 of its CTAs empty on the mixed batch)
+    if (n_tiles <= 0) return;
+    adjoint_kernel<<<n_tiles, kAdjointPoints, 0, s>>>(b, dL_dE, dL_dV, offsets_dev, tiles_dev, b.psi, 0);
 }
 
 }  // namespace epscu

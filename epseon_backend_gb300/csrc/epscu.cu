@@ -86,6 +86,8 @@ struct epscu_ctx {
     int last_method = 0;
     bool last_psi = false;
     int64_t* last_offsets_dev = nullptr;
+    int32_t* last_tiles_dev = nullptr;  // the adjoint's tile prefix over the potentials
+    int32_t last_n_tiles = 0;
     int64_t last_total_points = 0;
     int64_t last_psi_total = 0;
     epscu_stats stats{};
@@ -439,7 +441,11 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     auto* hm = (PotMeta*)ctx->host("meta", sizeof(PotMeta) * n, &ce);
     auto* ho = (int32_t*)ctx->host("order", sizeof(int32_t) * n, &ce);
     auto* hoff = (int64_t*)ctx->host("offsets", sizeof(int64_t) * n, &ce);
-    if (!hm || !ho || !hoff) return fail(EPSCU_ERR_NOMEM, "pinned staging allocation failed");
+    // the adjoint's CTAs: tiles of kAdjointPoints points of each potential, in
+    // potential order (htile[p] = the first tile of potential p)
+    auto* htile = (int32_t*)ctx->host("adj_tiles", sizeof(int32_t) * (n + 1), &ce);
+    if (!hm || !ho || !hoff || !htile) return fail(EPSCU_ERR_NOMEM, "pinned staging allocation failed");
+    htile[0] = 0;
     for (int p = 0; p < n; ++p) {
         const int32_t N = batch->N[p];
         const int64_t off = batch->offsets[p];
@@ -458,6 +464,7 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
         m.n_trial = batch->n_trial;
         hm[p] = m;
         hoff[p] = off;
+        htile[p + 1] = htile[p] + (N + kAdjointPoints - 1) / kAdjointPoints;
         total_points = std::max<int64_t>(total_points, off + N);
         total_padded += ((N + tile - 1) / tile) * tile;
         max_N = std::max(max_N, N);
@@ -519,9 +526,10 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
         }
     }
     int64_t* d_off = (int64_t*)ctx->get("offsets", sizeof(int64_t) * n, &ce);
+    int32_t* d_tiles = (int32_t*)ctx->get("adj_tiles", sizeof(int32_t) * (n + 1), &ce);
     if (ce != cudaSuccess || !b.meta || !b.W64 || !b.Msuf || !b.counts || !b.levels || !b.fallback_list || !b.units ||
         !b.hdr ||
-        !b.order || !d_off ||
+        !b.order || !d_off || !d_tiles ||
         (method == EPSCU_METHOD_FAST_FP32C && !b.Wf2))
         return fail(EPSCU_ERR_NOMEM, std::string("device arena: ") + cudaGetErrorString(ce));
     if (dev) {
@@ -638,6 +646,8 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
         if ((e = cudaMemcpyAsync(b.meta, hm, sizeof(PotMeta) * n, cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
         if ((e = cudaMemcpyAsync(b.order, ho, sizeof(int32_t) * n, cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
         if ((e = cudaMemcpyAsync(d_off, hoff, sizeof(int64_t) * n, cudaMemcpyHostToDevice, s)) != cudaSuccess) return e;
+        if ((e = cudaMemcpyAsync(d_tiles, htile, sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice, s)) != cudaSuccess)
+            return e;
         if ((e = cudaMemsetAsync(b.hdr, 0, sizeof(Header), s)) != cudaSuccess) return e;
         if (b.Wf2 && (e = cudaMemsetAsync(b.Wf2, 0, sizeof(float2) * total_padded, s)) != cudaSuccess) return e;
         return cudaSuccess;
@@ -814,6 +824,8 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     ctx->last_method = method;
     ctx->last_psi = psi_on && hh->error == 0;
     ctx->last_offsets_dev = d_off;
+    ctx->last_tiles_dev = d_tiles;
+    ctx->last_n_tiles = htile[n];
     ctx->last_total_points = total_points;
     ctx->last_psi_total = psi_total;
 
@@ -873,7 +885,7 @@ extern "C" epscu_status epscu_adjoint(epscu_ctx* ctx, const double* dL_dE, doubl
         gE = d_gE;
         gV = d_gV;
     }
-    launch_adjoint(b, gE, gV, ctx->last_total_points, ctx->last_offsets_dev, recompute, ctx->sm_count, s);
+    launch_adjoint(b, gE, gV, ctx->last_offsets_dev, ctx->last_tiles_dev, ctx->last_n_tiles, s);
     EPSCU_CU(cudaGetLastError());
     if (!dev) EPSCU_CU(cudaMemcpyAsync(dL_dV, gV, sizeof(double) * ctx->last_total_points, cudaMemcpyDeviceToHost, s));
     EPSCU_CU(cudaEventRecord(ctx->ev_out, s));

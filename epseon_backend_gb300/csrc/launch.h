@@ -135,8 +135,10 @@ void launch_refine_mid(const DevBatch& b, int sm_count, cudaStream_t s);
 void launch_norm_mid(const DevBatch& b, int sm_count, cudaStream_t s);
 
 // adjoint.cu
-void launch_adjoint(const DevBatch& b, const double* dL_dE, double* dL_dV, int64_t total_points,
-                    const int64_t* offsets_dev, int recompute, int sm_count, cudaStream_t s);
+// points per CTA of the adjoint (one thread each)
+constexpr int kAdjointPoints = 256;
+void launch_adjoint(const DevBatch& b, const double* dL_dE, double* dL_dV, const int64_t* offsets_dev,
+                    const int32_t* tiles_dev, int32_t n_tiles, cudaStream_t s);
 
 void launch_adjoint_explicit(int32_t n, int32_t cap, int32_t max_N, const int64_t* offsets, const int32_t* N,
                              const double* h, const int32_t* n_out, const int64_t* psi_off, const double* psi,
