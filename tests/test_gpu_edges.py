@@ -100,7 +100,8 @@ def test_psi_buffer_too_small(ctx, method):
 
 def test_bisection_scan_batch(ctx):
     """A batch large enough for the bisection scan (counts only where they
-    change: the coarse grid of every 8th trial energy, then halved cells)
+    change: the coarse grid of every 16th trial energy, then a count round
+    inside the cells whose end counts differ)
     gives every level of the plain FP64 solver (itself bit-exact with the
     oracle) within the fast method's tolerance, with its node count."""
     b = synth.mixed_batch(B=640, n_min=2048, n_max=6144, seed=11)

@@ -208,8 +208,9 @@ def test_long_grid_top_levels(ctx, method):
 
 def test_mixed_batch_path_with_psi(ctx):
     """The path the 2048-potential mixed batch takes, at its sizes: the first
-    512 potentials of that batch (enough for the bisection scan: every 8th
-    trial energy, then halved cells), 8192 trial energies, grids of 2048 to
+    512 potentials of that batch (enough for the bisection scan: every 16th
+    trial energy, then a count round inside the cells where the count
+    changes), 8192 trial energies, grids of 2048 to
     65,536 points, long level windows on one CTA per level.  A seeded sample
     of 24 potentials, 8 of each kind (for each kind its three longest grids,
     so LJ and N > 32k are in it, and five drawn at random), is compared with
