@@ -43,9 +43,9 @@ CPU_SAMPLE = 96  # potentials of the workload the CPU legs time
 # point, ncu on the 128-potential mixed batch (18.12 MB / 2,242,300 points)
 SCAN32_DRAM_BYTES_PER_POINT = 8.08
 # ncu (dram__bytes_read.sum + dram__bytes_write.sum) of refine_long_kernel per
-# algorithmic point-update on the 512-potential mixed batch (54.70 MB over
-# 147,450,449 point-updates: the windows' W is re-read from L2)
-REFINE_LONG_DRAM_BYTES_PER_UPDATE = 0.371
+# algorithmic point-update on the 512-potential mixed batch (64.05 MB over
+# 235,987,411 point-updates: the windows' W is re-read from L2)
+REFINE_LONG_DRAM_BYTES_PER_UPDATE = 0.2714
 
 
 def dist_env():
