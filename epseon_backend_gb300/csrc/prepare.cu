@@ -1,9 +1,9 @@
 // prepare.cu -- per-potential set-up of the discrete problem, level-slot
 // bookkeeping and device-side tabulation of parametric potentials.
 //
-// The set-up mirrors the oracle's eo_prepare() exactly (same FP64 operations):
-// minimum of V, E-independent Dirichlet cut-offs (a (V_i - E_lo) <= 1/2),
-// scan twist index (argmin V), trial spacing and the bisection step count.
+// The set-up gives the oracle's eo_prepare() results exactly: minimum of V,
+// E-independent Dirichlet cut-offs (a (V_i - E_lo) <= 1/2 in FP64), scan
+// twist index (first argmin of V), trial spacing and the bisection step count.
 #include <cuda_runtime.h>
 #include <math.h>
 
@@ -34,9 +34,6 @@ __device__ T block_reduce(T v, Op op, T* sh) {
     return v;
 }
 
-struct MinOp {
-    __device__ double operator()(double a, double b) const { return fmin(a, b); }
-};
 struct MinI {
     __device__ int operator()(int a, int b) const { return min(a, b); }
 };
@@ -58,31 +55,89 @@ __device__ __forceinline__ double dkey_inv(unsigned long long k) {
     const unsigned long long u = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
     return __longlong_as_double((long long)u);
 }
+// the same with the two zeros on one key (they compare equal as doubles)
+__device__ __forceinline__ unsigned long long dkey0(double x) {
+    unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    if ((u << 1) == 0ull) u = 0ull;
+    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+struct MinU {
+    __device__ unsigned long long operator()(unsigned long long a, unsigned long long b) const { return min(a, b); }
+};
+
+// (__double2float_rn(w), __double2float_rn(w - hi)) with integer operations
+// for 2^-60 <= |w| < 2^101 (the conversions otherwise): hi rounds the 52-bit
+// significand to 23 bits to nearest, ties to even; w - hi is the signed
+// remainder of the 29 dropped bits times 2^(e-52), exact in a double, so one
+// integer-to-float rounding of the remainder and two exact power-of-two
+// scalings give the same float as converting w - hi.  No FP64 instruction.
+__device__ __forceinline__ float2 split_double_rn(double w) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(w);
+    const int e = (int)((u >> 52) & 0x7ffull) - 1023;
+    if (e < -60 || e > 100) {
+        const float hi = __double2float_rn(w);
+        return make_float2(hi, __double2float_rn(__dsub_rn(w, (double)hi)));
+    }
+    const uint32_t sgn = (uint32_t)(u >> 32) & 0x80000000u;
+    const unsigned long long mant = u & 0xfffffffffffffull;
+    const uint32_t r = (uint32_t)(mant & 0x1fffffffull);
+    uint32_t hb = ((uint32_t)(e + 127) << 23) | (uint32_t)(mant >> 29);
+    const uint32_t up = (r > 0x10000000u || (r == 0x10000000u && (hb & 1u))) ? 1u : 0u;
+    hb += up;  // a carry out of the significand raises the exponent
+    const int rr = (int)r - (up ? 0x20000000 : 0);
+    float lo = 0.0f;
+    if (rr != 0) {
+        lo = __fmul_rn(__fmul_rn(__int2float_rn(rr), 2.220446049250313e-16f), __int_as_float((127 + e) << 23));
+        if (sgn) lo = -lo;
+    }
+    return make_float2(__uint_as_float(sgn | hb), lo);
+}
 
 __global__ void __launch_bounds__(kPrepThreads) prepare_kernel(DevBatch b) {
-    __shared__ double shd[32];
     __shared__ int shi[32];
+    __shared__ unsigned long long shk[32];
+    __shared__ unsigned long long s_kt;
     const int p = b.order[blockIdx.x];  // longest grids first (the tail is the last CTAs)
     PotMeta m = b.meta[p];
     const double* V = b.V64 + m.off;
     const int N = m.N;
     const int tid = threadIdx.x, nt = blockDim.x;
 
-    double vmin = INFINITY;
+    // The per-point comparisons run on order-preserving integer images of the
+    // doubles (dkey0), exact and on the integer pipes: min V and its finiteness,
+    // the cut-off test a (V_i - V_min) <= 1/2 (monotone in V_i, so it holds
+    // exactly up to a threshold image found once per potential by bisection
+    // on the images with the FP64 test itself) and the first argmin; the only
+    // FP64 instruction per point is W = a V.
+    unsigned long long kmin = kKeyMax;
     int bad = 0;
     for (int i = tid; i < N; i += nt) {
         const double v = V[i];
-        if (!isfinite(v)) bad = 1;
-        vmin = fmin(vmin, v);
+        if ((((unsigned long long)__double_as_longlong(v) >> 52) & 0x7ffull) == 0x7ffull) bad = 1;  // inf, NaN
+        else kmin = min(kmin, dkey0(v));
     }
-    vmin = block_reduce(vmin, MinOp(), shd);
+    kmin = block_reduce(kmin, MinU(), shk);
     bad = block_reduce(bad, OrI(), shi);
+    const double vmin = dkey_inv(kmin);
 
     const double h = __ddiv_rn(__dsub_rn(m.r_max, m.r_min), (double)(N - 1));
     const double a = __ddiv_rn(__dmul_rn(__dmul_rn(m.mu, h), h), 6.0);
+    if (tid == 0) {
+        // the largest image whose double passes the cut-off test (the test
+        // holds at V_min; the images above +inf are NaNs, which fail it)
+        unsigned long long lo = kmin, hi = kKeyMax;
+        while (hi - lo > 1ull) {
+            const unsigned long long mid = lo + (hi - lo) / 2;
+            if (__dmul_rn(a, __dsub_rn(dkey_inv(mid), vmin)) <= 0.5) lo = mid;
+            else hi = mid;
+        }
+        s_kt = lo;
+    }
+    __syncthreads();
+    const unsigned long long kt = s_kt;
     int first = N, last = -1;
     for (int i = tid; i < N; i += nt) {
-        if (__dmul_rn(a, __dsub_rn(V[i], vmin)) <= 0.5) {
+        if (dkey0(V[i]) <= kt) {
             first = min(first, i);
             last = max(last, i);
         }
@@ -93,17 +148,17 @@ __global__ void __launch_bounds__(kPrepThreads) prepare_kernel(DevBatch b) {
     const int i1 = last > N - 2 ? N - 2 : last;
 
     // argmin on [i0, i1], first occurrence
-    double bv = INFINITY;
+    unsigned long long bk = kKeyMax;
     int bi = N;
     for (int i = i0 + tid; i <= i1; i += nt) {
-        const double v = V[i];
-        if (v < bv) {
-            bv = v;
+        const unsigned long long k = dkey0(V[i]);
+        if (k < bk) {
+            bk = k;
             bi = i;
         }
     }
-    const double gmin = block_reduce(bv, MinOp(), shd);
-    int cand = (bv == gmin) ? bi : N;
+    const unsigned long long gk = block_reduce(bk, MinU(), shk);
+    int cand = (bk == gk) ? bi : N;
     const int k_scan = block_reduce(cand, MinI(), shi);
 
     // W = a V in FP64 and as an unevaluated (hi, lo) float pair; zero padding
@@ -112,11 +167,7 @@ __global__ void __launch_bounds__(kPrepThreads) prepare_kernel(DevBatch b) {
     for (int i = tid; i < N; i += nt) {
         const double w = __dmul_rn(a, V[i]);
         W[i] = w;
-        if (Wf) {
-            const float hi = __double2float_rn(w);
-            const float lo = __double2float_rn(__dsub_rn(w, (double)hi));
-            Wf[i] = make_float2(hi, lo);
-        }
+        if (Wf) Wf[i] = split_double_rn(w);
     }
 
     // Suffix minima of V on [i0, i1] (M), and for the fast method prefix
