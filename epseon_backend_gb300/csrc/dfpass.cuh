@@ -21,7 +21,10 @@ namespace epscu {
 // long levels on their own stream beside the lane kernels and FP32 passes on
 // the CTA path: the 2048-potential batch (93k levels) is fastest at 8192, the
 // 256-potential bump batch (14k levels) at 2048, the 64-Morse batch (3.4k
-// levels) at 1024-1536.  DevBatch::long_window > 0 overrides it.
+// levels) at 1024-1536.  With the fallback levels and the psi zeroing on the
+// long levels' stream the 2048-potential batch measured 28.6 / 27.4 / 27.2 /
+// 27.3 ms a step at 6144 / 8192 / 10240 / 12288 points (flat from 8192 up).
+// DevBatch::long_window > 0 overrides it.
 constexpr int kLongWindow = 8192;
 constexpr int kLongWindowLevels = 60000;
 constexpr int kMinLongWindow = 1024;
