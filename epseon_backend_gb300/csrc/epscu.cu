@@ -487,6 +487,8 @@ extern "C" epscu_status epscu_solve(epscu_ctx* ctx, const epscu_batch* batch, ep
     b.Msuf = (double*)ctx->get("Msuf", sizeof(double) * total_points, &ce);
     b.Wf2 = method == EPSCU_METHOD_FAST_FP32C ? (float2*)ctx->get("Wf2", sizeof(float2) * total_padded, &ce) : nullptr;
     b.counts = (int32_t*)ctx->get("counts", sizeof(int32_t) * (size_t)n * batch->n_trial, &ce);
+    b.gam = method == EPSCU_METHOD_FAST_FP32C ? (float*)ctx->get("gam", sizeof(float) * (size_t)n * batch->n_trial, &ce)
+                                              : nullptr;
     b.levels = (LevelWork*)ctx->get("levels", sizeof(LevelWork) * lv, &ce);
     b.fallback_list = (int32_t*)ctx->get("fallback_list", sizeof(int32_t) * lv, &ce);
     b.max_units = (int32_t)(n + lv / 32 + 1);

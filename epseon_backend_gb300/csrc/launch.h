@@ -21,6 +21,8 @@ struct DevBatch {
     float* Bmin;               // minima of W over 32-point blocks (index offf / 32 + block; fast method)
     float2* Wf2;               // a V as (hi, lo) floats, tile-aligned per potential
     int32_t* counts;           // [n * n_trial]
+    float* gam;                // [n * n_trial] the scan's matching function f_k gamma_k at the counted trial
+                               // energies (fast method: the refinement's first energy), or nullptr
     LevelWork* levels;         // [max_levels]
     int32_t* fallback_list;    // [max_levels] slots handed to the bisection fallback
     int2* units;               // [max_units] (first slot, count) per warp work unit

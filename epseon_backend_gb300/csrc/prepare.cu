@@ -428,6 +428,18 @@ __global__ void bracket_kernel(DevBatch b) {
             w.hi = trial_energy(m, top);
             w.E = __dmul_rn(0.5, __dadd_rn(w.lo, w.hi));
             w.n_in_bracket = c[top] - (lo == 0 ? 0 : c[lo - 1]);
+            if (b.gam && lo > 0 && w.n_in_bracket == 1) {
+                // the first energy of the refinement: the zero of the scan's
+                // matching function interpolated between the bracket's ends,
+                // when it falls from positive to negative there (one level, no
+                // pole between); the midpoint otherwise
+                const float* g = b.gam + (int64_t)p * b.n_trial;
+                const float gl = g[lo - 1], gr = g[top];
+                if (gl > 0.0f && gr < 0.0f && gl < INFINITY && gr > -INFINITY) {
+                    const double t = fmin(0.95, fmax(0.05, (double)gl / ((double)gl - (double)gr)));
+                    w.E = w.lo + t * (w.hi - w.lo);
+                }
+            }
         }
         w.lo0 = w.lo;
         w.hi0 = w.hi;

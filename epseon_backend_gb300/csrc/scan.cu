@@ -408,7 +408,10 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
         const double AC = uA * vC;
         const double num = -12.0 * Tk * AC + fk * ((double)Do * vC + (double)D * uA);
         nodes += (num < 0.0) != (AC < 0.0);
-        if (valid) b.counts[(int64_t)p * b.n_trial + j] = nodes;
+        if (valid) {
+            b.counts[(int64_t)p * b.n_trial + j] = nodes;
+            if (b.gam) b.gam[(int64_t)p * b.n_trial + j] = (float)(num / AC);
+        }
     }
     __syncthreads();
     if (s_abort && tid == 0) {
@@ -635,7 +638,10 @@ __global__ void __launch_bounds__(kCountThreads) count_list_kernel(DevBatch b) {
             const double AC = uA * vC;
             const double num = -12.0 * Tk * AC + fk * ((double)D * vC + (double)s_D[e] * uA);
             nodes += s_nodes[e] + ((num < 0.0) != (AC < 0.0));
-            if (j >= 0) b.counts[(int64_t)p * b.n_trial + j] = nodes;
+            if (j >= 0) {
+                b.counts[(int64_t)p * b.n_trial + j] = nodes;
+                if (b.gam) b.gam[(int64_t)p * b.n_trial + j] = (float)(num / AC);
+            }
         }
     }
 }
