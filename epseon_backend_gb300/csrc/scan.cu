@@ -441,6 +441,33 @@ __global__ void __launch_bounds__(THREADS) scan32_kernel(DevBatch b, int ipp, in
 constexpr int kCountThreads = 128;
 constexpr int kCountEnergies = kCountThreads / 2;
 
+// Exclusive prefix sum of v over the CTA (blockDim.x a multiple of 32, at
+// most 1024 threads); *total gets the sum.  Every thread must call it.
+__device__ __forceinline__ int block_exclusive_scan(int v, int* total) {
+    __shared__ int s_warp[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int t = lane < nw ? s_warp[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        if (lane < nw) s_warp[lane] = t;  // inclusive over the warps
+    }
+    __syncthreads();
+    const int before = (warp > 0 ? s_warp[warp - 1] : 0) + x - v;
+    *total = s_warp[nw - 1];
+    __syncthreads();  // s_warp is reused by the next call
+    return before;
+}
+
 __global__ void __launch_bounds__(256) bisect_plan_kernel(DevBatch b, int W, int split) {
     __shared__ int s_n;
     const int p = b.order[blockIdx.x];
@@ -450,24 +477,40 @@ __global__ void __launch_bounds__(256) bisect_plan_kernel(DevBatch b, int W, int
     int32_t* list = b.bis_list + (int64_t)p * b.n_trial;
     const int32_t* c = b.counts + (int64_t)p * b.n_trial;
     const int last = b.n_trial - 1;
+    // the list is in ascending trial order, written at prefix-sum offsets: a
+    // chunk of the count round (and so the window its energies march) is the
+    // same from run to run, and with it the matching function stored beside
+    // each count (atomic list positions made the refinement's first energies,
+    // and the final energies' last bits, vary between runs)
     if (!(m.status & EPSCU_STATUS_BAD)) {
         if (W == 0) {
             const int K = (b.n_trial + kBisectCoarse - 1) / kBisectCoarse;
-            for (int k = 1 + threadIdx.x; k <= K; k += blockDim.x) list[atomicAdd(&s_n, 1)] = min(k * kBisectCoarse - 1, last);
+            for (int k = 1 + threadIdx.x; k <= K; k += blockDim.x) list[k - 1] = min(k * kBisectCoarse - 1, last);
+            if (threadIdx.x == 0) s_n = K;
         } else {
             const int ncell = (b.n_trial + W - 1) / W;
-            for (int t = threadIdx.x; t < ncell; t += blockDim.x) {
-                const int a = t * W - 1;  // cell (a, a + W], count(-1) = 0
-                const int ca = a < 0 ? 0 : c[a];
-                const int cb = c[min(a + W, last)];
-                // a coarse cell with one level is cut into kBisectSingle parts
-                const int parts = (cb - ca == 1 && W == kBisectCoarse) ? min(kBisectSingle, split) : split;
-                if (ca >= 0 && cb > ca)
-                    for (int q = 1; q < parts; ++q) {
-                        const int pt = a + q * (W / parts);
-                        if (pt < last) list[atomicAdd(&s_n, 1)] = pt;
-                    }
+            int base = 0;
+            for (int t0 = 0; t0 < ncell; t0 += blockDim.x) {
+                const int t = t0 + threadIdx.x;
+                int a = 0, parts = 0, n_pts = 0;
+                if (t < ncell) {
+                    a = t * W - 1;  // cell (a, a + W], count(-1) = 0
+                    const int ca = a < 0 ? 0 : c[a];
+                    const int cb = c[min(a + W, last)];
+                    // a coarse cell with one level is cut into kBisectSingle parts
+                    parts = (cb - ca == 1 && W == kBisectCoarse) ? min(kBisectSingle, split) : split;
+                    if (ca >= 0 && cb > ca)
+                        for (int q = 1; q < parts; ++q) n_pts += (a + q * (W / parts) < last) ? 1 : 0;
+                }
+                int total = 0;
+                int at = base + block_exclusive_scan(n_pts, &total);
+                for (int q = 1; q < parts && n_pts > 0; ++q) {
+                    const int pt = a + q * (W / parts);
+                    if (pt < last) list[at++] = pt;
+                }
+                base += total;
             }
+            if (threadIdx.x == 0) s_n = base;
         }
     }
     __syncthreads();
