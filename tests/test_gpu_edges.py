@@ -109,6 +109,10 @@ def test_bisection_scan_batch(ctx):
     Vs = b.potentials()
     ref = ctx.solve(Vs, b.r_min, b.r_max, b.mu, b.e_cap, b.n_trial, method=capi.METHOD_PLAIN_FP64, level_capacity=256)
     sol = ctx.solve(Vs, b.r_min, b.r_max, b.mu, b.e_cap, b.n_trial, method=capi.METHOD_FAST_FP32C, level_capacity=256)
+    # a second solve gives the same bits (the count round's lists, and so the
+    # refinement's first energies, do not depend on thread scheduling)
+    again = ctx.solve(Vs, b.r_min, b.r_max, b.mu, b.e_cap, b.n_trial, method=capi.METHOD_FAST_FP32C, level_capacity=256)
+    assert np.array_equal(again.energy, sol.energy, equal_nan=True)
     assert np.array_equal(sol.n_total, ref.n_total)
     assert np.array_equal(sol.n_out, ref.n_out)
     checked = 0
